@@ -1,0 +1,364 @@
+"""Benchmark of the CSG ray-casting hot path on one GB300 (or N replicas under torchrun).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl engine|reference]
+
+A step is one primary-ray render (ray generation, Kensler traversal, intersections, Phong
+shading) of one view: by default the 512-sphere cheese scene at 3840x2160 (configuration
+2 of the benchmark set).  Prints one JSON line (rank 0).
+
+engine arm: value = rays / device time with the scene resident in HBM and the RGBA8 frame
+written to device memory; the L2 is flushed (256 MiB write) before every step.  e2e is
+the same metric through the C ABI with the frame copied to pinned host memory inside
+the timed region.  Also reported: the FP32 roofline of the render kernel (algorithmic
+FP32 operations of the reference algorithm on these rays / kernel time, against the
+measured FP32 FMA rate), the reference's own CUDA kernel on the same frame, and the CPU
+restatement of the reference on the host cores.
+
+reference arm (--impl reference): the reference's traversal/shading restated in C
+(oracle/, pinned bit-exact to the reference's host build) on all host cores, each step a
+bounded pixel sample of the same frame.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+sys.path.insert(0, str(ROOT / "cuda-csg-tree-raycasting_gb300"))
+
+METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() \
+    else "Mrays/s on 1 GB300"
+PEAKS = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+WORKLOADS = {
+    1: "testWikipedia tree (9 nodes), 1280x720, camera (0,0,5) fov 60, light (-1,-1,-1)",
+    2: "cheese: Difference(Cube edge 2, balanced Union of 512 spheres), 1025 nodes, 3840x2160, "
+       "seeded look-at camera at distance 4, fov 60",
+    3: "random CSG tree (seed 0: log-uniform 2..4096 leaves, depth <= 12), 1920x1080, seeded look-at camera",
+}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_scene_and_view(config: int, seed: int = 0):
+    from csgrt import scenes
+    text = scenes.config_scene_text(config, seed)
+    view = scenes.config_views(config, seed)[0]
+    return text, view
+
+
+def algorithmic_flops_per_ray(text, view, stride=8):
+    """Mean FP32 operations per ray of the reference algorithm on this view, counted by
+    the oracle (pinned to the reference) on every stride-th pixel in x and y."""
+    from oracle import Oracle
+    import csgrt
+    O = Oracle()
+    nodes, prims = O.parse(text)
+    w, h = view.w, view.h
+    ys = np.arange(stride // 2, h, stride)
+    xs = np.arange(stride // 2, w, stride)
+    pix = (ys[:, None] * w + xs[None, :]).ravel()
+    thf = csgrt.device_tan_half_fov(float(view.camera[5])) if _has_gpu() else None
+    out = O.render_list(nodes, prims, view.camera, view.light, w, h, pix, mode="fma", tan_half_fov=thf,
+                        want=(), counts=True)
+    c = out["counts"]
+    return float(c["flops"].mean()), float(c["flops_trace"].mean()), int(len(pix))
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+def cpu_baseline(text, view, seconds=10.0, nthreads=None, seed=0):
+    """The oracle (the reference's algorithm restated in C, pinned bit-exact to the
+    reference's host build) on a random pixel sample of the frame, all host threads."""
+    from oracle import Oracle
+    O = Oracle()
+    nodes, prims = O.parse(text)
+    nthreads = nthreads or os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    npix = view.w * view.h
+    n = 20000
+    pix = rng.integers(0, npix, n)
+    t0 = time.perf_counter()
+    O.render_list(nodes, prims, view.camera, view.light, view.w, view.h, pix, nthreads=nthreads, want=("rgba8",))
+    dt = time.perf_counter() - t0
+    rate = n / max(dt, 1e-9)
+    n2 = int(min(max(rate * seconds, 1000), 50_000_000))
+    pix = rng.integers(0, npix, n2)
+    t0 = time.perf_counter()
+    O.render_list(nodes, prims, view.camera, view.light, view.w, view.h, pix, nthreads=nthreads, want=("rgba8",))
+    dt = time.perf_counter() - t0
+    return {"value": n2 / dt / 1e6, "unit": "Mrays/s", "cores": nthreads, "kind": "port",
+            "sample": f"{n2} uniformly random pixels of the same frame, {dt:.1f} s on {nthreads} threads"}
+
+
+def reference_cuda(text, view, reps=3):
+    """The reference's own RaycastKernel + LightningKernel (nvcc, sm_103a) on the frame."""
+    from oracle import RefCuda
+    if not RefCuda.available():
+        return None
+    import csgrt
+    nodes44, prims48, _ = csgrt.parse_tree(text)
+    G = RefCuda()
+    out = G.render(nodes44, prims48, view.camera, view.light, view.w, view.h, reps=reps, want_hits=False,
+                   want_rgba=False)
+    rays = view.w * view.h
+    return {"value": rays / (out["ms_frame"] * 1e-3) / 1e6, "unit": "Mrays/s", "ms_frame": out["ms_frame"],
+            "ms_raycast_kernel": out["ms_ray"], "ms_lightning_kernel": out["ms_light"],
+            "note": "reference kernels as Raycaster::Raycast launches them (8x4 blocks, device sync after each)"}
+
+
+def traffic_from_profiles(kernel_key: str):
+    f = ROOT / "profiles" / "traffic.json"
+    if not f.exists():
+        return None
+    try:
+        d = json.loads(f.read_text())
+        return d.get(kernel_key)
+    except Exception:
+        return None
+
+
+def run_engine(args):
+    import torch
+    import csgrt
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    text, view = load_scene_and_view(args.config)
+    w, h = view.w, view.h
+    rays = w * h
+    scene = csgrt.Scene(text)
+    cam = csgrt.Camera.from_floats(view.camera)
+    stream = torch.cuda.current_stream()
+    out = torch.empty(rays, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def step():
+        scene.render_ptrs(cam, view.light, w, h, rgba8=out.data_ptr(), stream=stream.cuda_stream)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+    if scene.check(stream.cuda_stream) != 0:
+        raise RuntimeError("rays stopped at the traversal iteration cap")
+
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        t_start.record(stream)
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(stream)
+            step()
+            ev[i][1].record(stream)
+        t_end.record(stream)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    total_ms = t_start.elapsed_time(t_end)
+    launch_ms = [a.elapsed_time(b) for a, b in ev]
+    if dist:
+        tt = torch.tensor([total_ms], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+
+    # end to end through the C ABI: render + copy of the frame to pinned host memory
+    host = torch.empty(rays, dtype=torch.int32, pin_memory=True)
+    e2e_steps = max(3, min(args.steps, 10))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        step()
+        host.copy_(out, non_blocking=True)
+        stream.synchronize()
+    e2e_s = time.perf_counter() - t0
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    value = ws * rays * args.steps / (total_ms * 1e-3) / 1e6
+    avg_launch_ms = float(np.mean(launch_ms))
+    res = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": WORKLOADS[args.config], "config_index": args.config, "width": w, "height": h,
+                   "rays_per_step": rays, "nodes": scene.info()["n_nodes"], "output": "RGBA8 device plane",
+                   "l2": "flushed before every step by a 256 MiB device write (inside the timed region)",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "kernel_ms": {"mean": avg_launch_ms, "min": float(np.min(launch_ms)), "max": float(np.max(launch_ms))},
+        "gpu_launches": args.steps,
+        "e2e": {"value": round(rays * e2e_steps / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 72,
+                "d2h_bytes_per_step": rays * 4,
+                "note": "csg_render_planes through the C ABI + D2H of the RGBA8 frame to pinned host memory, "
+                        "wall clock; scene resident (uploaded once, as Raycaster::ChangeSize does)"},
+    }
+    clocks = clk.summary()
+    res["clocks"] = clocks
+
+    if not args.no_roofline:
+        flops_ray, flops_trace_ray, nsample = algorithmic_flops_per_ray(text, view)
+        peak = csgrt.probe_fp32_peak()
+        achieved = flops_ray * rays / (avg_launch_ms * 1e-3) / 1e12
+        res["roofline"] = {
+            "bound": "fp32", "achieved": round(achieved, 3), "peak": round(peak, 2), "unit": "TFLOP/s",
+            "frac": round(achieved / peak, 4),
+            "traffic": traffic_from_profiles(f"render_kernel/config{args.config}"),
+            "algorithmic_flops_per_ray": round(flops_ray, 1),
+            "flops_convention": "FP32 operations of the reference source on each ray's executed path "
+                                "(+ - * / sqrt min max pow tan = 1, a*b+c as written = 2), counted by the "
+                                f"oracle on {nsample} sampled rays",
+            "peak_source": "measured FP32 FMA rate (csg_probe_fp32_peak, FMA = 2 FLOP) on this GPU",
+            "hbm": {"achieved_gbs": round(rays * 4 / (avg_launch_ms * 1e-3) / 1e9, 2),
+                    "peak_gbs": PEAKS.get("hbm_gbs"), "peak_source": "MEASURED_PEAKS.json hbm_gbs",
+                    "algorithmic_bytes_per_ray": 4},
+        }
+    if not args.no_reference_cuda:
+        rc = reference_cuda(text, view)
+        if rc:
+            rc["engine_speedup"] = round(value / ws / rc["value"], 2)
+            res["reference_cuda"] = rc
+    if not args.no_cpu_baseline:
+        res["cpu_baseline"] = cpu_baseline(text, view, seconds=args.cpu_seconds)
+    scene.close()
+    print(json.dumps(res), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    text, view = load_scene_and_view(args.config)
+    per_step_s = max(0.5, min(args.cpu_seconds / 4, 8.0))
+    for _ in range(args.warmup):
+        cpu_baseline(text, view, seconds=0.2)
+    vals = []
+    t0 = time.perf_counter()
+    samples = []
+    for i in range(args.steps):
+        r = cpu_baseline(text, view, seconds=per_step_s, seed=i + 1)
+        vals.append(r["value"])
+        samples.append(r["sample"])
+    total = time.perf_counter() - t0
+    value = float(np.mean(vals))
+    res = {"metric": METRIC, "value": round(value, 4), "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(1000 * total / args.steps, 2), "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+           "impl": "reference",
+           "config": {"workload": WORKLOADS[args.config], "config_index": args.config, "width": view.w,
+                      "height": view.h},
+           "cpu_baseline": {"value": round(value, 4), "unit": "Mrays/s", "cores": os.cpu_count(), "kind": "port",
+                            "sample": f"per step: {samples[0]}"},
+           "e2e": {"value": round(value, 4), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "note": "the reference's host build cannot run on this machine (its sources are not here); the C "
+                   "restatement pinned bit-exact to it on the reference's own scenes is timed instead"}
+    print(json.dumps(res), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-reference-cuda", action="store_true")
+    ap.add_argument("--no-roofline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_engine(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,287 @@
+"""Python bindings (ctypes) of libcsgrt, the GB300 CSG ray-casting engine.
+
+Thin mirror of the C ABI in ``include/csgrt.h`` for tests and benchmarks.  Device
+buffers are plain device pointers (``torch.Tensor.data_ptr()`` works); the library is
+the only compute path -- :func:`lib` raises if ``libcsgrt.so`` has not been built, and
+nothing here falls back to a CPU implementation.
+
+Mirrors of the reference interface:
+
+* :class:`Scene` -- ``CSGTree::Parse`` + ``Raycaster::ChangeSize``'s upload
+  (CSGTree.cu:5-179, Raycaster.cu:3-21); raises :class:`CsgError` with the reference's
+  parse message on bad input.
+* :class:`Camera` -- the reference ``Camera`` (Camera.h / Camera.cpp), same byte layout.
+* :func:`light_dir` -- ``DirectionalLight::getLightDir`` (DirectionalLight.h:13-18).
+* :meth:`Scene.render` -- ``Raycaster::Raycast`` (Raycaster.cu:23-34).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+from pathlib import Path
+
+import numpy as np
+
+PKG_DIR = Path(__file__).resolve().parent.parent
+LIB_PATH = PKG_DIR / "_build" / "libcsgrt.so"
+
+CSG_OK, CSG_E_PARSE, CSG_E_RANGE, CSG_E_COUNT, CSG_E_CUDA = 0, 1, 2, 3, 4
+CSG_E_BUDGET, CSG_E_TIMEOUT, CSG_E_DEPTH, CSG_E_ARG, CSG_E_CAPACITY = 5, 6, 7, 8, 9
+
+# Every symbol include/csgrt.h (and include/csgrt_batch.h) declares.
+EXPORTED = [
+    "csg_abi_version", "csg_status_string",
+    "csg_tree_parse", "csg_scene_create", "csg_scene_destroy", "csg_scene_get_info", "csg_scene_export_reference_layout",
+    "csg_camera_init", "csg_camera_set_position", "csg_camera_set_rotation", "csg_camera_set_fov",
+    "csg_camera_move", "csg_camera_rotate", "csg_light_dir", "csg_light_default",
+    "csg_render", "csg_render_f4", "csg_render_planes", "csg_scene_check", "csg_device_tan_half_fov",
+    "csg_probe_fp32_peak",
+]
+
+_vp = ctypes.c_void_p
+_f = ctypes.c_float
+_i32 = ctypes.c_int32
+
+
+class CsgError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"csg status {code}: {msg}")
+        self.code = code
+        self.msg = msg
+
+
+class csg_camera(ctypes.Structure):
+    _fields_ = [("x", _f), ("y", _f), ("z", _f), ("rot_x", _f), ("rot_y", _f), ("fov", _f),
+                ("forward", _f * 3), ("right", _f * 3), ("up", _f * 3)]
+
+
+class csg_scene_info(ctypes.Structure):
+    _fields_ = [("n_nodes", _i32), ("n_prims", _i32), ("op_depth", _i32), ("stack_class", _i32),
+                ("device_bytes", ctypes.c_uint64)]
+
+
+class csg_planes(ctypes.Structure):
+    _fields_ = [("rgba8", _vp), ("rgba32f", _vp), ("t", _vp), ("prim", _vp), ("normal", _vp)]
+
+
+_LIB = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load libcsgrt.so (built by build_lib.py).  Raises if it is missing."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = os.environ.get("CSGRT_LIB", str(LIB_PATH))
+    if not os.path.exists(path):
+        raise RuntimeError(f"libcsgrt.so not built ({path}); run __graft_entry__.build()")
+    L = ctypes.CDLL(path)
+    L.csg_abi_version.restype = ctypes.c_int
+    L.csg_status_string.argtypes = [ctypes.c_int]
+    L.csg_status_string.restype = ctypes.c_char_p
+    L.csg_scene_create.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp), ctypes.c_char_p,
+                                   ctypes.c_size_t]
+    L.csg_scene_destroy.argtypes = [_vp]
+    L.csg_tree_parse.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _vp, _i32, _vp, _i32, ctypes.POINTER(_i32),
+                                 ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.c_char_p, ctypes.c_size_t]
+    L.csg_scene_get_info.argtypes = [_vp, ctypes.POINTER(csg_scene_info)]
+    L.csg_scene_export_reference_layout.argtypes = [_vp, _vp, _i32, _vp, _i32, ctypes.POINTER(_i32),
+                                                    ctypes.POINTER(_i32)]
+    C = ctypes.POINTER(csg_camera)
+    L.csg_camera_init.argtypes = [C]
+    L.csg_camera_set_position.argtypes = [C, _f, _f, _f]
+    L.csg_camera_set_rotation.argtypes = [C, _f, _f]
+    L.csg_camera_set_fov.argtypes = [C, _f]
+    L.csg_camera_move.argtypes = [C, _f, _f, _f]
+    L.csg_camera_rotate.argtypes = [C, _f, _f]
+    for n in ("csg_camera_init", "csg_camera_set_position", "csg_camera_set_rotation", "csg_camera_set_fov",
+              "csg_camera_move", "csg_camera_rotate", "csg_light_dir", "csg_light_default"):
+        getattr(L, n).restype = None
+    L.csg_light_dir.argtypes = [_f, _f, ctypes.POINTER(_f)]
+    L.csg_light_default.argtypes = [ctypes.POINTER(_f)]
+    L.csg_render.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp, _vp, _vp, _vp]
+    L.csg_render_f4.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
+    L.csg_render_planes.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, ctypes.POINTER(csg_planes), _vp]
+    L.csg_scene_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
+    L.csg_device_tan_half_fov.argtypes = [_f, ctypes.POINTER(_f)]
+    L.csg_probe_fp32_peak.argtypes = [ctypes.POINTER(_f), ctypes.POINTER(_f)]
+    _LIB = L
+    return L
+
+
+def device_tan_half_fov(fov: float) -> float:
+    out = _f()
+    check(lib().csg_device_tan_half_fov(fov, ctypes.byref(out)))
+    return out.value
+
+
+def probe_fp32_peak() -> float:
+    """Measured FP32 FMA rate of the current GPU in TFLOP/s."""
+    tf, ms = _f(), _f()
+    check(lib().csg_probe_fp32_peak(ctypes.byref(tf), ctypes.byref(ms)))
+    return tf.value
+
+
+def status_string(code: int) -> str:
+    return lib().csg_status_string(code).decode()
+
+
+def check(code: int, msg: str = ""):
+    if code != CSG_OK:
+        raise CsgError(code, msg or status_string(code))
+
+
+def parse_tree(text: str | bytes):
+    """CSGTree::Parse on the host: (nodes, prims, op_depth) with nodes and prims as raw
+    bytes in the reference's 44-byte CSGNode / 48-byte Primitive layouts."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    nn, npr, dep = _i32(), _i32(), _i32()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().csg_tree_parse(data, len(data), None, 0, None, 0, ctypes.byref(nn), ctypes.byref(npr),
+                              ctypes.byref(dep), err, 512)
+    if rc != CSG_OK:
+        raise CsgError(rc, err.value.decode(errors="replace"))
+    nodes = np.zeros(nn.value * 44, np.uint8)
+    prims = np.zeros(npr.value * 48, np.uint8)
+    check(lib().csg_tree_parse(data, len(data), nodes.ctypes.data, nn.value, prims.ctypes.data, npr.value,
+                               ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep), err, 512))
+    return nodes, prims, dep.value
+
+
+# ------------------------------------------------------------------------------------
+class Camera:
+    """The reference Camera (Camera.h:3-53): position, pitch/yaw, fov, cached basis."""
+
+    def __init__(self):
+        self.c = csg_camera()
+        lib().csg_camera_init(ctypes.byref(self.c))
+
+    @classmethod
+    def from_floats(cls, v) -> "Camera":
+        cam = cls()
+        arr = np.ascontiguousarray(v, np.float32)
+        ctypes.memmove(ctypes.byref(cam.c), arr.ctypes.data, 60)
+        return cam
+
+    def floats(self) -> np.ndarray:
+        return np.frombuffer(bytes(self.c), np.float32).copy()
+
+    def set_position(self, x, y, z):
+        lib().csg_camera_set_position(ctypes.byref(self.c), x, y, z)
+        return self
+
+    def set_rotation(self, pitch, yaw):
+        lib().csg_camera_set_rotation(ctypes.byref(self.c), pitch, yaw)
+        return self
+
+    def set_fov(self, degrees):
+        lib().csg_camera_set_fov(ctypes.byref(self.c), degrees)
+        return self
+
+    def move(self, fwd, right, up):
+        lib().csg_camera_move(ctypes.byref(self.c), fwd, right, up)
+        return self
+
+    def rotate(self, dpitch, dyaw):
+        lib().csg_camera_rotate(ctypes.byref(self.c), dpitch, dyaw)
+        return self
+
+    @classmethod
+    def look_at_origin(cls, direction, distance=4.0, fov_deg=60.0) -> "Camera":
+        """Camera at distance * unit(direction), looking at the origin: pitch = asin(-p.y),
+        yaw = atan2(p.x, p.z) (forward = (-sin yaw cos pitch, sin pitch, -cos yaw cos pitch))."""
+        d = np.asarray(direction, np.float64)
+        d = d / np.linalg.norm(d)
+        cam = cls()
+        p = distance * d
+        cam.set_position(float(np.float32(p[0])), float(np.float32(p[1])), float(np.float32(p[2])))
+        cam.set_rotation(float(np.float32(math.asin(-d[1]))), float(np.float32(math.atan2(d[0], d[2]))))
+        cam.set_fov(fov_deg)
+        return cam
+
+
+def light_dir(polar=None, azimuth=None) -> np.ndarray:
+    out = (_f * 3)()
+    if polar is None:
+        lib().csg_light_default(out)
+    else:
+        lib().csg_light_dir(polar, azimuth, out)
+    return np.array(list(out), np.float32)
+
+
+# ------------------------------------------------------------------------------------
+class Scene:
+    """A parsed, device-resident CSG scene (opaque handle)."""
+
+    def __init__(self, text: str | bytes):
+        data = text.encode() if isinstance(text, str) else bytes(text)
+        h = _vp()
+        err = ctypes.create_string_buffer(512)
+        rc = lib().csg_scene_create(data, len(data), ctypes.byref(h), err, 512)
+        if rc != CSG_OK:
+            raise CsgError(rc, err.value.decode(errors="replace"))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().csg_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self) -> dict:
+        inf = csg_scene_info()
+        check(lib().csg_scene_get_info(self.h, ctypes.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in csg_scene_info._fields_}
+
+    def export_reference_layout(self):
+        """(nodes, prims) as raw bytes in the reference's CSGNode / Primitive layouts."""
+        nn, npr = _i32(), _i32()
+        check(lib().csg_scene_export_reference_layout(self.h, None, 0, None, 0, ctypes.byref(nn),
+                                                      ctypes.byref(npr)))
+        nodes = np.zeros(nn.value * 44, np.uint8)
+        prims = np.zeros(npr.value * 48, np.uint8)
+        check(lib().csg_scene_export_reference_layout(self.h, nodes.ctypes.data, nn.value, prims.ctypes.data,
+                                                      npr.value, ctypes.byref(nn), ctypes.byref(npr)))
+        return nodes, prims
+
+    def render_ptrs(self, cam: Camera, light, w: int, h: int, rgba8=0, rgba32f=0, t=0, prim=0, normal=0,
+                    stream=0):
+        light = (_f * 3)(*[float(v) for v in light])
+        pl = csg_planes(rgba8 or None, rgba32f or None, t or None, prim or None, normal or None)
+        check(lib().csg_render_planes(self.h, ctypes.byref(cam.c), light, w, h, ctypes.byref(pl),
+                                      stream or None))
+
+    def render_torch(self, cam: Camera, light, w: int, h: int, planes=("rgba8",), stream=None, out=None):
+        """Render into torch CUDA tensors; returns a dict of the requested planes."""
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+        n = w * h
+        out = dict(out or {})
+        spec = {"rgba8": (n,), "rgba32f": (n, 4), "t": (n,), "prim": (n,), "normal": (3, n)}
+        dts = {"rgba8": torch.int32, "rgba32f": torch.float32, "t": torch.float32, "prim": torch.int32,
+               "normal": torch.float32}
+        for k in planes:
+            if k not in out:
+                out[k] = torch.empty(spec[k], dtype=dts[k], device=dev)
+        st = stream if stream is not None else torch.cuda.current_stream()
+        self.render_ptrs(cam, light, w, h, **{k: out[k].data_ptr() for k in planes}, stream=st.cuda_stream)
+        return out
+
+    def check(self, stream=0) -> int:
+        n = ctypes.c_uint64()
+        rc = lib().csg_scene_check(self.h, stream or None, ctypes.byref(n))
+        if rc not in (CSG_OK, CSG_E_TIMEOUT):
+            check(rc)
+        return int(n.value)

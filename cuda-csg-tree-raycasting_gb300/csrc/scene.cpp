@@ -1,0 +1,321 @@
+// Scene text parser, bounding boxes and device-layout packer.
+//
+// Behaviour follows CSGTree::Parse (CSGRayCasting/Graphics/RayCasting/CSGTree/CSGTree.cu:5-152):
+// whitespace tokens in preorder; an operator's first child becomes `left`, its second
+// `right`; primitive parameters are read with the same C conversions std::stof / stod /
+// stoi use, in the same order, so the same text produces the same bits and the same
+// first error.  Where the reference indexes past the end of the token list (undefined
+// behaviour) this parser reports CSG_E_PARSE instead.
+#include "scene.hpp"
+
+#include <cerrno>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+
+namespace csgrt {
+namespace {
+
+bool is_space(char c)
+{
+    return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r';
+}
+
+std::vector<std::string_view> tokenize(std::string_view text)
+{
+    std::vector<std::string_view> toks;
+    size_t i = 0;
+    while (i < text.size()) {
+        while (i < text.size() && is_space(text[i])) ++i;
+        if (i >= text.size()) break;
+        size_t j = i;
+        while (j < text.size() && !is_space(text[j])) ++j;
+        toks.emplace_back(text.substr(i, j - i));
+        i = j;
+    }
+    return toks;
+}
+
+// std::stof: strtof, "no conversion" -> invalid_argument("stof"), ERANGE -> out_of_range.
+int to_float(std::string_view tok, float& v, std::string& err)
+{
+    std::string s(tok);
+    char* end = nullptr;
+    const int saved = errno;
+    errno = 0;
+    v = std::strtof(s.c_str(), &end);
+    const int e = errno;
+    errno = saved;
+    if (end == s.c_str()) { err = "stof"; return kErrParse; }
+    if (e == ERANGE) { err = "stof"; return kErrRange; }
+    return kOk;
+}
+
+int to_double(std::string_view tok, double& v, std::string& err)
+{
+    std::string s(tok);
+    char* end = nullptr;
+    const int saved = errno;
+    errno = 0;
+    v = std::strtod(s.c_str(), &end);
+    const int e = errno;
+    errno = saved;
+    if (end == s.c_str()) { err = "stod"; return kErrParse; }
+    if (e == ERANGE) { err = "stod"; return kErrRange; }
+    return kOk;
+}
+
+// color(): std::stoi(two hex characters, nullptr, 16) / 255 (CSGTree.cu:196-200).
+int to_channel(std::string_view two, float& v, std::string& err)
+{
+    std::string s(two);
+    char* end = nullptr;
+    const int saved = errno;
+    errno = 0;
+    const long x = std::strtol(s.c_str(), &end, 16);
+    const int e = errno;
+    errno = saved;
+    if (end == s.c_str()) { err = "stoi"; return kErrParse; }
+    if (e == ERANGE || x < INT32_MIN || x > INT32_MAX) { err = "stoi"; return kErrRange; }
+    v = static_cast<float>(static_cast<int>(x)) / 255;
+    return kOk;
+}
+
+// Cylinder axis (Primitives.h:54-88): R(rotX, rotY, rotZ) * (0, 1, 0) in double,
+// divided by its squared length, rounded to float.
+void cylinder_axis(double rx, double ry, double rz, float* axis)
+{
+    const double deg = 0.017453292519943295769236907684886;
+    rx = rx * deg;
+    ry = ry * deg;
+    rz = rz * deg;
+    double x = -std::sin(rz) * std::cos(ry) + std::sin(ry) * std::sin(rx) * std::cos(rz);
+    double y = std::cos(rx) * std::cos(rz);
+    double z = std::sin(ry) * std::sin(rz) + std::sin(rx) * std::cos(ry) * std::cos(rz);
+    const double len2 = (x * x + y * y + z * z);
+    x /= len2;
+    y /= len2;
+    z /= len2;
+    axis[0] = static_cast<float>(x);
+    axis[1] = static_cast<float>(y);
+    axis[2] = static_cast<float>(z);
+}
+
+// Leaf bounding boxes (BVHNode.cuh:17-52): sphere +-2r as (c - r) - r, cylinder
+// +-max(h/2, r), cube +-edge/2.
+void leaf_box(RefNode& n, const RefPrim& p)
+{
+    const float c[3] = {p.x, p.y, p.z};
+    float lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    if (n.type == kSphere) {
+        const float r = p.p[0];
+        for (int k = 0; k < 3; ++k) { lo[k] = c[k] - r - r; hi[k] = c[k] + r + r; }
+    } else if (n.type == kCylinder) {
+        const float h2 = p.p[1] / 2, r = p.p[0];
+        const float m = (h2 < r) ? r : h2;
+        for (int k = 0; k < 3; ++k) { lo[k] = c[k] - m; hi[k] = c[k] + m; }
+    } else if (n.type == kCube) {
+        const float hs = p.p[0] / 2;
+        for (int k = 0; k < 3; ++k) { lo[k] = c[k] - hs; hi[k] = c[k] + hs; }
+    }
+    n.minx = lo[0]; n.miny = lo[1]; n.minz = lo[2];
+    n.maxx = hi[0]; n.maxy = hi[1]; n.maxz = hi[2];
+}
+
+// Operator boxes (BVHNode.cuh:54-63) with std::min / std::max semantics.
+inline float min_ref(float a, float b) { return (b < a) ? b : a; }
+inline float max_ref(float a, float b) { return (a < b) ? b : a; }
+
+void build_boxes(HostTree& t)
+{
+    // Children always follow their parent in preorder, so a reverse sweep visits every
+    // child before its parent.
+    for (int i = static_cast<int>(t.nodes.size()) - 1; i >= 0; --i) {
+        RefNode& n = t.nodes[i];
+        if (n.prim != -1) {
+            leaf_box(n, t.prims[n.prim]);
+        } else {
+            const RefNode& l = t.nodes[n.left];
+            const RefNode& r = t.nodes[n.right];
+            n.minx = min_ref(l.minx, r.minx); n.miny = min_ref(l.miny, r.miny);
+            n.minz = min_ref(l.minz, r.minz);
+            n.maxx = max_ref(l.maxx, r.maxx); n.maxy = max_ref(l.maxy, r.maxy);
+            n.maxz = max_ref(l.maxz, r.maxz);
+        }
+    }
+}
+
+int32_t operator_depth(const HostTree& t)
+{
+    std::vector<int32_t> d(t.nodes.size(), 0);
+    int32_t best = 0;
+    for (size_t i = 0; i < t.nodes.size(); ++i) {
+        const RefNode& n = t.nodes[i];
+        const int32_t here = (n.parent >= 0 ? d[n.parent] : 0) + (n.prim == -1 ? 1 : 0);
+        d[i] = here;
+        if (here > best) best = here;
+    }
+    return best;
+}
+
+}  // namespace
+
+int parse_tree(std::string_view text, HostTree& out, std::string& err)
+{
+    out = HostTree{};
+    err.clear();
+    const std::vector<std::string_view> toks = tokenize(text);
+    struct Open { int32_t node; int32_t children; };
+    std::vector<Open> open;
+    auto& nodes = out.nodes;
+    auto& prims = out.prims;
+    nodes.reserve(toks.size());
+
+    for (size_t i = 0; i < toks.size(); ++i) {
+        const int32_t id = static_cast<int32_t>(nodes.size());
+        nodes.push_back(RefNode{-1, -1, -1, -1, -1, 0, 0, 0, 0, 0, 0});
+        if (id != 0) {
+            if (open.empty()) { err = "Cannot parse"; return kErrParse; }
+            Open& top = open.back();
+            nodes[id].parent = top.node;
+            if (top.children == 0) {
+                nodes[top.node].left = id;
+                top.children = 1;
+            } else {
+                nodes[top.node].right = id;
+                open.pop_back();
+            }
+        }
+        const std::string_view kw = toks[i];
+        int32_t type;
+        if (kw == "Union") type = kUnion;
+        else if (kw == "Difference") type = kDifference;
+        else if (kw == "Intersection") type = kIntersection;
+        else if (kw == "Sphere") type = kSphere;
+        else if (kw == "Cylinder") type = kCylinder;
+        else if (kw == "Cube") type = kCube;
+        else {
+            err = "Cannot parse - Unrecognized keyword: " + std::string(kw);
+            return kErrParse;
+        }
+        nodes[id].type = type;
+        if (type <= kIntersection) {
+            open.push_back({id, 0});
+            continue;
+        }
+
+        auto param = [&](size_t k, std::string_view& tok) -> bool {
+            if (i + k >= toks.size()) {
+                err = "Cannot parse - missing parameters after " + std::string(kw);
+                return false;
+            }
+            tok = toks[i + k];
+            return true;
+        };
+        RefPrim p{};
+        p.id = static_cast<int32_t>(prims.size());
+        std::string_view tok;
+        float xyz[3];
+        for (int k = 0; k < 3; ++k) {
+            if (!param(1 + k, tok)) return kErrParse;
+            if (int rc = to_float(tok, xyz[k], err)) return rc;
+        }
+        if (!param(4, tok)) return kErrParse;
+        if (tok.size() != 6) {
+            err = "Cannot parse color " + std::string(tok);
+            return kErrParse;
+        }
+        float rgb[3];
+        for (int k = 0; k < 3; ++k)
+            if (int rc = to_channel(tok.substr(2 * k, 2), rgb[k], err)) return rc;
+        p.x = xyz[0]; p.y = xyz[1]; p.z = xyz[2];
+        p.r = rgb[0]; p.g = rgb[1]; p.b = rgb[2];
+        size_t consumed = 5;
+        if (type == kSphere || type == kCube) {
+            if (!param(5, tok)) return kErrParse;
+            if (int rc = to_float(tok, p.p[0], err)) return rc;
+        } else {
+            if (!param(5, tok)) return kErrParse;
+            if (int rc = to_float(tok, p.p[0], err)) return rc;
+            if (!param(6, tok)) return kErrParse;
+            if (int rc = to_float(tok, p.p[1], err)) return rc;
+            double rot[3];
+            for (int k = 0; k < 3; ++k) {
+                if (!param(7 + k, tok)) return kErrParse;
+                if (int rc = to_double(tok, rot[k], err)) return rc;
+            }
+            static const char* const kRotMsg[3] = {
+                "Invalid roation rotX should be in range [0, 360] deg",
+                "Invalid roation rotY should be in range [0, 360] deg",
+                "Invalid roation rotZ should be in range [0, 360] deg"};
+            for (int k = 0; k < 3; ++k)
+                if (rot[k] > 360 || rot[k] < 0) { err = kRotMsg[k]; return kErrRange; }
+            cylinder_axis(rot[0], rot[1], rot[2], &p.p[2]);
+            consumed = 9;
+        }
+        nodes[id].prim = p.id;
+        prims.push_back(p);
+        i += consumed;
+    }
+    if (nodes.size() != 2 * prims.size() - 1 || prims.empty()) {
+        err = "Cannot parse - number of primitives do not match number of nodes";
+        return kErrCount;
+    }
+    if (prims.size() > 32767) {
+        // RayHitMinimal keeps the primitive index in a short (Ray.cuh:36-52).
+        err = "scene has more than 32767 primitives";
+        return kErrDepth;
+    }
+    build_boxes(out);
+    out.op_depth = operator_depth(out);
+    return kOk;
+}
+
+int32_t stack_class_for_depth(int32_t op_depth)
+{
+    if (op_depth <= 4) return 4;
+    if (op_depth <= 8) return 8;
+    if (op_depth <= 12) return 12;
+    if (op_depth <= 15) return 16;
+    return 32;
+}
+
+namespace {
+inline float as_float(int32_t v)
+{
+    float f;
+    std::memcpy(&f, &v, 4);
+    return f;
+}
+}  // namespace
+
+void pack_scene(const HostTree& t, PackedScene& out)
+{
+    const size_t n = t.nodes.size(), np = t.prims.size();
+    out.topo.assign(n, int4{0, 0, 0, 0});
+    out.kids.assign(4 * n, float4{0, 0, 0, 0});
+    out.geo.assign(2 * np, float4{0, 0, 0, 0});
+    out.color.assign(np, float4{0, 0, 0, 0});
+    for (size_t i = 0; i < n; ++i) {
+        const RefNode& nd = t.nodes[i];
+        if (nd.prim != -1) {
+            out.topo[i] = int4{nd.prim, -1, nd.parent, nd.type};
+            continue;
+        }
+        out.topo[i] = int4{nd.left, nd.right, nd.parent, nd.type};
+        const RefNode& l = t.nodes[nd.left];
+        const RefNode& r = t.nodes[nd.right];
+        out.kids[4 * i + 0] = float4{l.minx, l.miny, l.minz, as_float(l.type)};
+        out.kids[4 * i + 1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
+        out.kids[4 * i + 2] = float4{r.minx, r.miny, r.minz, as_float(r.type)};
+        out.kids[4 * i + 3] = float4{r.maxx, r.maxy, r.maxz, as_float(r.prim)};
+    }
+    for (size_t i = 0; i < np; ++i) {
+        const RefPrim& p = t.prims[i];
+        out.geo[2 * i + 0] = float4{p.x, p.y, p.z, p.p[0]};
+        out.geo[2 * i + 1] = float4{p.p[1], p.p[2], p.p[3], p.p[4]};
+        out.color[i] = float4{p.r, p.g, p.b, 0.f};
+    }
+}
+
+}  // namespace csgrt

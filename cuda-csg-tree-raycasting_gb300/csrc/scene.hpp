@@ -1,0 +1,86 @@
+// Scene model of the CSG ray-casting engine: the host tree parsed from the reference's
+// text format, and the flattened device layout the kernels read.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <string_view>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+namespace csgrt {
+
+// CSGTree::NodeType (CSGTree.cuh:38-46).
+enum NodeType : int32_t { kUnion = 0, kDifference = 1, kIntersection = 2,
+                          kSphere = 3, kCylinder = 4, kCube = 5 };
+
+// Host records in the reference's own byte layouts, so a parsed tree can be exported
+// to (and compared with) the reference: CSGNode (CSGTree.cuh:15-34, with the BVHNode of
+// BVHNode.cuh:6-11 embedded) and Primitive (Primitives.h:29-40).
+struct RefNode {
+    int32_t type, prim, left, right, parent;
+    float minx, miny, minz, maxx, maxy, maxz;
+};
+struct RefPrim {
+    int32_t id;
+    float x, y, z;
+    float r, g, b;
+    float p[5];  // sphere: radius | cylinder: radius, height, axis xyz | cube: edge
+};
+static_assert(sizeof(RefNode) == 44, "CSGNode layout");
+static_assert(sizeof(RefPrim) == 48, "Primitive layout");
+
+struct HostTree {
+    std::vector<RefNode> nodes;  // node 0 is the root, preorder
+    std::vector<RefPrim> prims;  // file order
+    int32_t op_depth = 0;        // most operator nodes on a root-to-leaf path
+};
+
+// Parse status codes (values of csg_status).
+enum : int { kOk = 0, kErrParse = 1, kErrRange = 2, kErrCount = 3, kErrDepth = 7 };
+
+// CSGTree::Parse (CSGTree.cu:5-152) followed by ConstructBVH (CSGTree.cu:154-179).
+// Returns a status code; `err` receives the reference's exception text.
+int parse_tree(std::string_view text, HostTree& out, std::string& err);
+
+// ---------------------------------------------------------------------------------
+// Device layout (all arrays 16-byte aligned, one cudaMalloc):
+//   topo[n]    int4   {left, right, parent, type} for operators,
+//                     {prim, -1, parent, type} for leaves
+//   kids[4n]   float4 for an operator node: its two children's boxes with the child's
+//                     type and primitive index in .w (as int bits):
+//                     {l.min.xyz, l.type} {l.max.xyz, l.prim} {r.min.xyz, r.type} {r.max.xyz, r.prim}
+//                     (the Ulyanov layout: everything GoTo needs at a node in four
+//                     independent 16-byte loads)
+//   geo[2p]    float4 {cx, cy, cz, p0} {p1, p2, p3, p4}
+//   color[p]   float4 {r, g, b, 0}
+// ---------------------------------------------------------------------------------
+struct DeviceScene {
+    const int4* topo = nullptr;
+    const float4* kids = nullptr;
+    const float4* geo = nullptr;
+    const float4* color = nullptr;
+    int32_t n_nodes = 0;
+    int32_t n_prims = 0;
+    int32_t op_depth = 0;
+    int32_t stack_class = 0;
+};
+
+// Host image of the device arrays (for upload and for tests).
+struct PackedScene {
+    std::vector<int4> topo;
+    std::vector<float4> kids;
+    std::vector<float4> geo;
+    std::vector<float4> color;
+};
+void pack_scene(const HostTree& tree, PackedScene& out);
+
+// Stack capacity class used by the kernels for a tree of this operator depth: the
+// per-ray primitive and time stacks never hold more entries than the operator depth,
+// and the action stack never more than 2 * depth + 1, so a tree with depth <= 15 never
+// reaches the reference's 32-entry limit (RaycastingKernels.cuh:19).  Deeper trees use
+// the 32-entry class, which reproduces the reference's drop-on-full behaviour.
+int32_t stack_class_for_depth(int32_t op_depth);
+
+}  // namespace csgrt

@@ -1,0 +1,141 @@
+/* csgrt -- GB300-native (sm_103a) CSG ray-casting engine, C ABI.
+ *
+ * Drop-in for the render path of Zumi002/CUDA-CSG-Tree-Raycasting: load a CSG tree
+ * from the reference's preorder text format, set a camera and a directional light, and
+ * ray-cast + Phong-shade into a caller-owned device buffer.  Plain pointers and sizes
+ * only; every call returns a csg_status.  No call exits the process, none synchronises
+ * the device unless its comment says so, and renders are ordered on the caller's stream.
+ *
+ * Reference interfaces replaced (file:line within the reference project):
+ *   CSGTree::Parse + ConstructBVH        CSGRayCasting/Graphics/RayCasting/CSGTree/CSGTree.cu:5-179
+ *   Raycaster::ChangeSize (scene upload) CSGRayCasting/Graphics/RayCasting/Raycaster.cu:3-21
+ *   Raycaster::Raycast                   CSGRayCasting/Graphics/RayCasting/Raycaster.cu:23-34
+ *   Raycaster::CleanUp                   CSGRayCasting/Graphics/RayCasting/Raycaster.cu:36-44
+ *   Camera                               CSGRayCasting/Graphics/RenderManager/Camera/Camera.h:3-53, Camera.cpp:4-36
+ *   DirectionalLight::getLightDir        CSGRayCasting/Graphics/RenderManager/DirectionalLight.h:8-18
+ */
+#ifndef CSGRT_H
+#define CSGRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CSGRT_ABI_VERSION 1
+
+/* Status codes.  Parse errors carry the reference's exception text in `err`. */
+typedef enum csg_status {
+    CSG_OK = 0,
+    CSG_E_PARSE = 1,    /* malformed scene text (std::invalid_argument in the reference) */
+    CSG_E_RANGE = 2,    /* number out of range, or a rotation outside [0, 360] degrees */
+    CSG_E_COUNT = 3,    /* node count != 2 * primitive count - 1 */
+    CSG_E_CUDA = 4,     /* a CUDA runtime call failed */
+    CSG_E_BUDGET = 5,   /* request refused: device-memory budget exceeded */
+    CSG_E_TIMEOUT = 6,  /* a bounded device wait gave up, or rays hit the iteration cap */
+    CSG_E_DEPTH = 7,    /* scene too large for the device layout (> 32767 primitives) */
+    CSG_E_ARG = 8,      /* invalid argument (null pointer, non-positive size, ...) */
+    CSG_E_CAPACITY = 9  /* caller-provided array too small */
+} csg_status;
+
+/* Same 60-byte layout as the reference's Camera (Camera.h:9-16), so a caller can pass
+ * the bytes of a reference Camera object directly. */
+typedef struct csg_camera {
+    float x, y, z;    /* position */
+    float rot_x;      /* pitch, radians */
+    float rot_y;      /* yaw, radians */
+    float fov;        /* vertical field of view, radians */
+    float forward[3];
+    float right[3];
+    float up[3];
+} csg_camera;
+
+typedef struct csg_scene csg_scene; /* opaque, device-resident until destroyed */
+
+typedef struct csg_scene_info {
+    int32_t n_nodes;      /* nodes in the tree (2 * n_prims - 1) */
+    int32_t n_prims;      /* primitives (sphere, cylinder, cube) */
+    int32_t op_depth;     /* most operator nodes on any root-to-leaf path */
+    int32_t stack_class;  /* per-ray stack capacity the kernels use for this scene */
+    uint64_t device_bytes;/* device memory held by the scene */
+} csg_scene_info;
+
+/* Optional per-pixel planes.  Any pointer may be NULL.  Row-major, w*h entries, row 0 is
+ * the image row the reference computes with v = 0.5/(h-1) (its GL texture's first row). */
+typedef struct csg_planes {
+    uint32_t* rgba8;   /* packed R | G<<8 | B<<16 | A<<24, q = lrintf(clamp(c,0,1)*255) */
+    float* rgba32f;    /* float4 per pixel: the reference's RGBA32F PBO format */
+    float* t;          /* hit distance, +inf on a miss */
+    int32_t* prim;     /* hit primitive index (file order), -1 on a miss */
+    float* normal;     /* three planes (x, y, z) of w*h floats; 0 on a miss */
+} csg_planes;
+
+/* ---- scene: CSGTree::Parse (CSGTree.cu:5-152) + ConstructBVH (CSGTree.cu:154-179) +
+ *      the scene upload of Raycaster::ChangeSize (Raycaster.cu:16-17) --------------- */
+/* Parses `len` bytes of scene text, builds the bounding boxes and the flattened device
+ * layout, uploads it on the current device, and synchronises that upload.  On failure
+ * *out is NULL and `err` (if given) holds the reference's message, e.g.
+ * "Cannot parse - Unrecognized keyword: Spere". */
+int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, size_t errlen);
+/* Frees the scene's device memory (Raycaster::CleanUp, Raycaster.cu:36-44). */
+int csg_scene_destroy(csg_scene* scene);
+int csg_scene_get_info(const csg_scene* scene, csg_scene_info* info);
+/* CSGTree::Parse alone (host only, no device work): parses and builds the boxes into the
+ * reference's own record layouts, 44-byte CSGNode (CSGTree.cuh:15-34) and 48-byte
+ * Primitive (Primitives.h:29-40).  Pass NULL arrays to query the counts.  Unused
+ * parameter slots of a primitive are zero. */
+int csg_tree_parse(const char* text, size_t len, void* nodes44, int32_t max_nodes, void* prims48,
+                   int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
+                   char* err, size_t errlen);
+/* Copies the parsed tree out in the reference's own record layouts: 44-byte CSGNode
+ * (CSGTree.cuh:15-34) and 48-byte Primitive (Primitives.h:29-40).  Pass NULL arrays to
+ * query the counts. */
+int csg_scene_export_reference_layout(const csg_scene* scene, void* nodes44, int32_t max_nodes,
+                                      void* prims48, int32_t max_prims,
+                                      int32_t* n_nodes, int32_t* n_prims);
+
+/* ---- camera and light: Camera (Camera.h, Camera.cpp), DirectionalLight ------------- */
+void csg_camera_init(csg_camera* cam);                       /* Camera() */
+void csg_camera_set_position(csg_camera* cam, float x, float y, float z);
+void csg_camera_set_rotation(csg_camera* cam, float pitch, float yaw); /* clamps pitch to +-89 deg */
+void csg_camera_set_fov(csg_camera* cam, float degrees);
+void csg_camera_move(csg_camera* cam, float forward, float right, float up);
+void csg_camera_rotate(csg_camera* cam, float dpitch, float dyaw);
+void csg_light_dir(float polar, float azimuth, float out[3]); /* radians */
+void csg_light_default(float out[3]);                         /* polar -60 deg, azimuth -45 deg */
+
+/* ---- render: Raycaster::Raycast (Raycaster.cu:23-34) = RaycastKernel + LightningKernel
+ *      fused into one launch on `stream` (a cudaStream_t; NULL = legacy default) -------- */
+/* One primary ray per pixel, Kensler single-hit CSG traversal, Phong shading.
+ * `light_dir` is the DirectionalLight direction (normalised inside, as the reference
+ * does).  All output pointers are device pointers owned by the caller. */
+int csg_render(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
+               int32_t w, int32_t h, uint32_t* rgba8_dev, float* t_dev, int32_t* prim_dev,
+               float* normal_dev, void* stream);
+/* The reference's own output format: w*h float4 RGBA32F. */
+int csg_render_f4(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
+                  int32_t w, int32_t h, float* rgba_f4_dev, void* stream);
+/* Every plane at once. */
+int csg_render_planes(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
+                      int32_t w, int32_t h, const csg_planes* planes, void* stream);
+/* Synchronises `stream` and reports how many rays of the renders issued since the last
+ * call stopped at the traversal iteration cap (CSG_E_TIMEOUT if any, else CSG_OK). */
+int csg_scene_check(const csg_scene* scene, void* stream, uint64_t* n_capped);
+
+/* ---- misc ---------------------------------------------------------------------------- */
+/* Diagnostic: tan(fov / 2) as the device's ray generation computes it (RaycastingKernels.cu
+ * :15-16 evaluates tan on the device).  Synchronous.  For checkers that restate the ray
+ * generation on a host, whose tanf may differ in the last bit. */
+int csg_device_tan_half_fov(float fov, float* out);
+/* Diagnostic: measures the FP32 fused-multiply-add rate of the current device (TFLOP/s,
+ * an FMA counted as 2), the denominator of the FP32 roofline.  Synchronous. */
+int csg_probe_fp32_peak(float* tflops, float* ms);
+const char* csg_status_string(int status);
+int csg_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CSGRT_H */

@@ -1,0 +1,66 @@
+"""The C ABI library loads and exports every function include/*.h declares (no compute
+calls: this runs without a GPU), and the host-only entry points behave."""
+from __future__ import annotations
+
+import ctypes
+import re
+
+import numpy as np
+
+from conftest import GOLDEN, ROOT
+
+
+def declared_functions() -> set[str]:
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        for m in re.finditer(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(csg_\w+)\s*\(", text, flags=re.M):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_every_declared_symbol(csg):
+    names = declared_functions()
+    assert len(names) >= 20
+    lib = csg.lib()
+    missing = [n for n in sorted(names) if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(csg.EXPORTED) <= names
+
+
+def test_status_strings_and_version(csg):
+    assert csg.lib().csg_abi_version() == 1
+    for code in range(10):
+        assert csg.status_string(code)
+
+
+def test_camera_matches_reference_bytes(csg):
+    data = np.load(GOLDEN / "ref_camera.npz")
+    eq = lambda a, b: (np.asarray(a, np.float32).view(np.uint32) == np.asarray(b, np.float32).view(np.uint32)).all()
+    assert eq(csg.Camera().floats(), data["default"])
+    assert eq(csg.Camera().set_fov(60).floats(), data["fov60"])
+    assert eq(csg.Camera().set_position(1, 2, 3).set_rotation(0.3, -1.2).set_fov(45).floats(), data["posrot"])
+    assert eq(csg.Camera().set_rotation(2.0, 7.0).floats(), data["clamped"])
+    assert eq(csg.Camera().set_fov(75).rotate(0.21, -0.33).move(0.7, -0.4, 0.25).floats(), data["moved"])
+    for i in range(16):
+        a = data[f"lookat{i}/args"]
+        c = csg.Camera().set_position(*map(float, a[:3])).set_rotation(float(a[3]), float(a[4])).set_fov(60)
+        assert eq(c.floats(), data[f"lookat{i}"])
+    assert eq(csg.light_dir(), data["light_default"])
+    assert eq(csg.light_dir(0.4, 1.1), data["light_custom"])
+
+
+def test_camera_struct_layout(csg):
+    assert ctypes.sizeof(csg.csg_camera) == 60
+    c = csg.Camera.from_floats(np.arange(15, dtype=np.float32))
+    assert (c.floats() == np.arange(15, dtype=np.float32)).all()
+
+
+def test_render_rejects_bad_arguments_without_gpu(csg):
+    lib = csg.lib()
+    cam = csg.Camera()
+    light = (ctypes.c_float * 3)(-1, -1, -1)
+    assert lib.csg_render(None, ctypes.byref(cam.c), light, 16, 16, None, None, None, None, None) == csg.CSG_E_ARG
+    assert lib.csg_scene_destroy(None) == csg.CSG_E_ARG
+    out = ctypes.c_void_p()
+    assert lib.csg_scene_create(None, 5, ctypes.byref(out), None, 0) == csg.CSG_E_ARG
