@@ -122,9 +122,10 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
     const size_t n = s->tree.nodes.size(), np = s->tree.prims.size();
     const size_t off_topo = 0;
     const size_t off_kids = align16(off_topo + n * sizeof(int4));
-    const size_t off_geo = align16(off_kids + 4 * n * sizeof(float4));
+    const size_t off_geo = align16(off_kids + pk.kids.size() * sizeof(float4));
     const size_t off_color = align16(off_geo + 2 * np * sizeof(float4));
-    const size_t off_status = align16(off_color + np * sizeof(float4));
+    const size_t off_bvh = align16(off_color + np * sizeof(float4));
+    const size_t off_status = align16(off_bvh + pk.bvh.size() * sizeof(float4));
     const size_t total = align16(off_status + sizeof(unsigned long long));
     cudaGetDevice(&s->device);
     cudaError_t e = cudaMalloc(&s->dmem, total);
@@ -136,7 +137,9 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
     char* base = static_cast<char*>(s->dmem);
     e = cudaMemcpy(base + off_topo, pk.topo.data(), n * sizeof(int4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
-        e = cudaMemcpy(base + off_kids, pk.kids.data(), 4 * n * sizeof(float4), cudaMemcpyHostToDevice);
+        e = cudaMemcpy(base + off_kids, pk.kids.data(), pk.kids.size() * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !pk.bvh.empty())
+        e = cudaMemcpy(base + off_bvh, pk.bvh.data(), pk.bvh.size() * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(base + off_geo, pk.geo.data(), 2 * np * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -157,6 +160,11 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
     s->dev.n_prims = static_cast<int32_t>(np);
     s->dev.op_depth = s->tree.op_depth;
     s->dev.stack_class = csgrt::stack_class_for_depth(s->tree.op_depth);
+    s->dev.bvh = reinterpret_cast<const float4*>(base + off_bvh);
+    s->dev.n_bvh = static_cast<int32_t>(pk.bvh.size() / 4);
+    s->dev.live_words = pk.live_words;
+    s->dev.live_shift = pk.live_shift;
+    s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
     s->status = reinterpret_cast<unsigned long long*>(base + off_status);
     *out = s;
     return CSG_OK;

@@ -1,15 +1,18 @@
 // Single-view render kernel: RaycastKernel + LightningKernel of the reference
 // (CSGRayCasting/Graphics/RayCasting/Kernels/RaycastingKernels.cu:3-111) fused into one
-// launch, one thread per pixel, shading in the traversal's epilogue.  Nothing passes
-// through global memory between the two stages (the reference round-trips a 36-byte
-// RayHit per pixel); the only HBM traffic is the output planes.
+// launch, one thread per pixel, each warp an 8x4 pixel tile, shading in the traversal's
+// epilogue.  Nothing passes through global memory between the two stages (the
+// reference round-trips a 36-byte RayHit per pixel); the only HBM traffic is the output
+// planes.  Each ray first finds the primitives it can hit at all (liveness pre-pass over
+// a BVH of the leaves), then runs the reference's traversal, skipping subtrees with no
+// live primitive left.
 #include "render.hpp"
 #include "trace.cuh"
 
 namespace csgrt {
 namespace {
 
-constexpr int kThreads = 128;  // 4 warps; each warp covers an 8x4 pixel tile
+constexpr int kThreads = 128;  // 4 warps
 constexpr int kTileW = 16, kTileH = 8;
 
 struct RenderParams {
@@ -22,33 +25,11 @@ struct RenderParams {
     uint32_t iter_cap;
 };
 
-template <int SD>
-__global__ void __launch_bounds__(kThreads) render_kernel(const RenderParams p)
+// Details, shading and the output planes of one finished ray.
+__device__ __forceinline__ void write_pixel(const RenderParams& p, const dev::Ray& ray, const dev::Hit& h,
+                                            bool capped, int x, int y)
 {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint16_t tab[27];
-    if (threadIdx.x < 27) tab[threadIdx.x] = dev::table_entry(threadIdx.x);
-
-    const int tid = threadIdx.x;
-    const int warp = tid >> 5, lane = tid & 31;
-    const int x = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
-
-    dev::SmemStacks<SD> st;
-    st.nt = kThreads;
-    st.tid = tid;
-    st.pt = reinterpret_cast<float*>(smem_raw);
-    st.pb = reinterpret_cast<uint32_t*>(st.pt + SD * kThreads);
-    st.tt = reinterpret_cast<float*>(st.pb + SD * kThreads);
-    __syncthreads();
-    if (x >= p.w || y >= p.h) return;
-
-    const float width = (float)p.w, height = (float)p.h;
-    const dev::Ray ray = dev::primary_ray(p.cam.v, x, y, width, height);
-    uint32_t iters = 0;
-    const dev::Hit h = dev::csg_traverse<SD>(p.scene, ray, st, tab, p.iter_cap, &iters);
-    if (iters > p.iter_cap) atomicAdd(p.status, 1ull);
-
+    if (capped) atomicAdd(p.status, 1ull);
     const long long pix = (long long)y * p.w + x;
     const long long npix = (long long)p.w * p.h;
     // A hit always carries the index of a primitive it was computed from; the range check
@@ -74,17 +55,73 @@ __global__ void __launch_bounds__(kThreads) render_kernel(const RenderParams p)
     }
 }
 
+// Shared memory of a block: the per-ray primitive and time stacks (SD slots), the per-ray
+// live masks (scene.live_words words) and one BVH stack per warp.
+template <int SD>
+__host__ __device__ constexpr size_t stack_bytes()
+{
+    return (size_t)SD * kThreads * 12;
+}
+inline size_t smem_bytes(int sd, int live_words)
+{
+    return (size_t)sd * kThreads * 12 + (size_t)live_words * kThreads * 4 +
+           (size_t)(kThreads / 32) * dev::kWarpStack * 4;
+}
+
+template <int SD>
+__global__ void __launch_bounds__(kThreads) render_tiled(const RenderParams p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint16_t tab[27];
+    if (threadIdx.x < 27) tab[threadIdx.x] = dev::table_entry(threadIdx.x);
+    const int tid = threadIdx.x;
+    dev::SmemStacks<SD> st;
+    st.nt = kThreads;
+    st.tid = tid;
+    st.pt = reinterpret_cast<float*>(smem_raw);
+    st.pb = reinterpret_cast<uint32_t*>(st.pt + SD * kThreads);
+    st.tt = reinterpret_cast<float*>(st.pb + SD * kThreads);
+    st.np = 0;
+    st.ntm = 0;
+    uint32_t* live_base = reinterpret_cast<uint32_t*>(smem_raw + stack_bytes<SD>());
+    int* wstacks = reinterpret_cast<int*>(live_base + (size_t)p.scene.live_words * kThreads);
+    dev::LiveMask lm;
+    lm.w = live_base + tid;
+    lm.nt = kThreads;
+    lm.shift = p.scene.live_shift;
+    lm.words = p.scene.live_words;
+    lm.sum = 0;
+
+    const int warp = tid >> 5, lane = tid & 31;
+    const int x = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
+    const int y = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
+    const bool inside = x < p.w && y < p.h;
+    __syncthreads();
+    const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h);
+    // every lane of the warp takes part in the pre-pass walk; lanes outside the image
+    // only follow it
+    dev::live_prepass(ray, inside, p.scene, lm, wstacks + warp * dev::kWarpStack);
+    if (!inside) return;
+    bool capped = false;
+    const dev::Hit h = dev::csg_traverse<SD>(p.scene, ray, st, tab, lm, p.iter_cap, &capped);
+    write_pixel(p, ray, h, capped, x, y);
+}
+
 template <int SD>
 cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
 {
-    const size_t smem = (size_t)SD * kThreads * 12;
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(render_kernel<SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)smem);
+    const size_t smem = smem_bytes(SD, p.scene.live_words);
+    // Above the default 48 KiB per block the kernel needs the opt-in; set it once for the
+    // largest layout any scene can ask for (kLiveWordsMax live words).
+    static bool attr_set = false;
+    if (!attr_set) {
+        const cudaError_t e = cudaFuncSetAttribute(render_tiled<SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)smem_bytes(SD, kLiveWordsMax));
         if (e != cudaSuccess) return e;
+        attr_set = true;
     }
     const dim3 grid((p.w + kTileW - 1) / kTileW, (p.h + kTileH - 1) / kTileH);
-    render_kernel<SD><<<grid, kThreads, smem, stream>>>(p);
+    render_tiled<SD><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 

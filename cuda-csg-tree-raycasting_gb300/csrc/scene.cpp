@@ -12,6 +12,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <utility>
 
 namespace csgrt {
 namespace {
@@ -268,8 +269,20 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err)
     }
     build_boxes(out);
     out.op_depth = operator_depth(out);
+    out.leaf_lo.assign(nodes.size(), 0);
+    out.leaf_hi.assign(nodes.size(), 0);
+    for (int i = static_cast<int>(nodes.size()) - 1; i >= 0; --i) {
+        if (nodes[i].prim != -1) {
+            out.leaf_lo[i] = out.leaf_hi[i] = nodes[i].prim;
+        } else {
+            out.leaf_lo[i] = out.leaf_lo[nodes[i].left];
+            out.leaf_hi[i] = out.leaf_hi[nodes[i].right];
+        }
+    }
     return kOk;
 }
+
+bool use_prepass(int32_t n_prims) { return n_prims >= 8; }
 
 int32_t stack_class_for_depth(int32_t op_depth)
 {
@@ -289,11 +302,142 @@ inline float as_float(int32_t v)
 }
 }  // namespace
 
+namespace {
+
+struct Box {
+    float lo[3], hi[3];
+};
+
+// Binned-SAH BVH over the leaves' boxes.  Each internal node stores both children's
+// boxes; a child that is a single leaf stores that leaf's own (reference) box, and an
+// internal child stores the exact min/max of its leaves' boxes, so every stored box
+// contains the boxes below it.
+struct BvhBuilder {
+    const std::vector<Box>& box;
+    const std::vector<int32_t>& type;
+    std::vector<float4>& out;
+    std::vector<int32_t> idx;
+
+    static float area(const Box& b)
+    {
+        const float dx = b.hi[0] - b.lo[0], dy = b.hi[1] - b.lo[1], dz = b.hi[2] - b.lo[2];
+        return dx * dy + dy * dz + dz * dx;
+    }
+    Box bounds(int a, int b) const
+    {
+        Box r{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+        for (int i = a; i < b; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const Box& x = box[idx[i]];
+                r.lo[k] = x.lo[k] < r.lo[k] ? x.lo[k] : r.lo[k];
+                r.hi[k] = x.hi[k] > r.hi[k] ? x.hi[k] : r.hi[k];
+            }
+        return r;
+    }
+    int split(int a, int b)
+    {
+        // centroid bounds
+        float clo[3] = {INFINITY, INFINITY, INFINITY}, chi[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (int i = a; i < b; ++i)
+            for (int k = 0; k < 3; ++k) {
+                const float c = 0.5f * (box[idx[i]].lo[k] + box[idx[i]].hi[k]);
+                clo[k] = c < clo[k] ? c : clo[k];
+                chi[k] = c > chi[k] ? c : chi[k];
+            }
+        constexpr int kBins = 16;
+        float best = INFINITY;
+        int best_axis = -1;
+        float best_cut = 0;
+        for (int k = 0; k < 3; ++k) {
+            const float ext = chi[k] - clo[k];
+            if (!(ext > 0)) continue;
+            int cnt[kBins] = {0};
+            Box bb[kBins];
+            for (auto& x : bb) x = Box{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}};
+            for (int i = a; i < b; ++i) {
+                const Box& x = box[idx[i]];
+                const float c = 0.5f * (x.lo[k] + x.hi[k]);
+                int bi = static_cast<int>((c - clo[k]) / ext * kBins);
+                bi = bi < 0 ? 0 : (bi >= kBins ? kBins - 1 : bi);
+                cnt[bi]++;
+                for (int q = 0; q < 3; ++q) {
+                    bb[bi].lo[q] = x.lo[q] < bb[bi].lo[q] ? x.lo[q] : bb[bi].lo[q];
+                    bb[bi].hi[q] = x.hi[q] > bb[bi].hi[q] ? x.hi[q] : bb[bi].hi[q];
+                }
+            }
+            for (int cut = 1; cut < kBins; ++cut) {
+                Box L{{INFINITY, INFINITY, INFINITY}, {-INFINITY, -INFINITY, -INFINITY}}, R = L;
+                int nl = 0, nr = 0;
+                for (int q = 0; q < kBins; ++q) {
+                    Box& T = q < cut ? L : R;
+                    (q < cut ? nl : nr) += cnt[q];
+                    if (!cnt[q]) continue;
+                    for (int z = 0; z < 3; ++z) {
+                        T.lo[z] = bb[q].lo[z] < T.lo[z] ? bb[q].lo[z] : T.lo[z];
+                        T.hi[z] = bb[q].hi[z] > T.hi[z] ? bb[q].hi[z] : T.hi[z];
+                    }
+                }
+                if (!nl || !nr) continue;
+                const float cost = area(L) * nl + area(R) * nr;
+                if (cost < best) {
+                    best = cost;
+                    best_axis = k;
+                    best_cut = clo[k] + ext * cut / kBins;
+                }
+            }
+        }
+        int mid = a;
+        if (best_axis >= 0) {
+            for (int i = a; i < b; ++i) {
+                const Box& x = box[idx[i]];
+                if (0.5f * (x.lo[best_axis] + x.hi[best_axis]) < best_cut) std::swap(idx[i], idx[mid++]);
+            }
+        }
+        if (mid == a || mid == b) mid = (a + b) / 2;  // degenerate: split by count
+        return mid;
+    }
+    static float as_float(int32_t v)
+    {
+        float f;
+        std::memcpy(&f, &v, 4);
+        return f;
+    }
+    void child(int node, int side, int a, int b, int32_t child_index)
+    {
+        const Box bb = bounds(a, b);
+        const bool leaf = (b - a == 1);
+        const int32_t c = leaf ? ~idx[a] : child_index;
+        const int32_t ty = leaf ? type[idx[a]] : -1;
+        out[4 * node + 2 * side + 0] = float4{bb.lo[0], bb.lo[1], bb.lo[2], as_float(c)};
+        out[4 * node + 2 * side + 1] = float4{bb.hi[0], bb.hi[1], bb.hi[2], as_float(ty)};
+    }
+    // Builds the node for leaves [a, b) (b - a >= 2) at index `node`.
+    void build(int node, int a, int b)
+    {
+        const int mid = split(a, b);
+        int lchild = -1, rchild = -1;
+        if (mid - a >= 2) {
+            lchild = static_cast<int>(out.size() / 4);
+            out.resize(out.size() + 4);
+        }
+        if (b - mid >= 2) {
+            rchild = static_cast<int>(out.size() / 4);
+            out.resize(out.size() + 4);
+        }
+        child(node, 0, a, mid, lchild);
+        child(node, 1, mid, b, rchild);
+        if (lchild >= 0) build(lchild, a, mid);
+        if (rchild >= 0) build(rchild, mid, b);
+    }
+};
+
+}  // namespace
+
 void pack_scene(const HostTree& t, PackedScene& out)
 {
     const size_t n = t.nodes.size(), np = t.prims.size();
     out.topo.assign(n, int4{0, 0, 0, 0});
-    out.kids.assign(4 * n, float4{0, 0, 0, 0});
+    out.kids.assign(kKidsPerNode * n, float4{0, 0, 0, 0});
     out.geo.assign(2 * np, float4{0, 0, 0, 0});
     out.color.assign(np, float4{0, 0, 0, 0});
     for (size_t i = 0; i < n; ++i) {
@@ -305,10 +449,35 @@ void pack_scene(const HostTree& t, PackedScene& out)
         out.topo[i] = int4{nd.left, nd.right, nd.parent, nd.type};
         const RefNode& l = t.nodes[nd.left];
         const RefNode& r = t.nodes[nd.right];
-        out.kids[4 * i + 0] = float4{l.minx, l.miny, l.minz, as_float(l.type)};
-        out.kids[4 * i + 1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
-        out.kids[4 * i + 2] = float4{r.minx, r.miny, r.minz, as_float(r.type)};
-        out.kids[4 * i + 3] = float4{r.maxx, r.maxy, r.maxz, as_float(r.prim)};
+        float4* k = &out.kids[kKidsPerNode * i];
+        k[0] = float4{l.minx, l.miny, l.minz, as_float(l.type)};
+        k[1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
+        k[2] = float4{r.minx, r.miny, r.minz, as_float(r.type)};
+        k[3] = float4{r.maxx, r.maxy, r.maxz, as_float(r.prim)};
+        k[4] = float4{as_float(t.leaf_lo[nd.left]), as_float(t.leaf_hi[nd.left]), as_float(t.leaf_lo[nd.right]),
+                      as_float(t.leaf_hi[nd.right])};
+    }
+    // live-mask granularity: one bit per 2^shift leaves, at most kLiveWordsMax words
+    int32_t shift = 0;
+    while (((static_cast<int64_t>(np) + (1 << shift) - 1) >> shift) > 32 * kLiveWordsMax) ++shift;
+    out.live_shift = shift;
+    out.live_words = static_cast<int32_t>((((np + (1u << shift) - 1) >> shift) + 31) / 32);
+    // BVH over the leaves' reference boxes (primitive order -> node order)
+    out.bvh.clear();
+    if (np >= 2) {
+        std::vector<Box> boxes(np);
+        std::vector<int32_t> types(np);
+        for (size_t i = 0; i < n; ++i) {
+            const RefNode& nd = t.nodes[i];
+            if (nd.prim == -1) continue;
+            boxes[nd.prim] = Box{{nd.minx, nd.miny, nd.minz}, {nd.maxx, nd.maxy, nd.maxz}};
+            types[nd.prim] = nd.type;
+        }
+        BvhBuilder b{boxes, types, out.bvh, {}};
+        b.idx.resize(np);
+        for (size_t i = 0; i < np; ++i) b.idx[i] = static_cast<int32_t>(i);
+        out.bvh.resize(4);
+        b.build(0, 0, static_cast<int>(np));
     }
     for (size_t i = 0; i < np; ++i) {
         const RefPrim& p = t.prims[i];

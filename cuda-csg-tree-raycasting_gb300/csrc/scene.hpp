@@ -35,6 +35,9 @@ struct HostTree {
     std::vector<RefNode> nodes;  // node 0 is the root, preorder
     std::vector<RefPrim> prims;  // file order
     int32_t op_depth = 0;        // most operator nodes on a root-to-leaf path
+    // Leaves are numbered in preorder, which is the primitive (file) order, so the leaves
+    // of every subtree form one contiguous primitive range [leaf_lo, leaf_hi].
+    std::vector<int32_t> leaf_lo, leaf_hi;
 };
 
 // Parse status codes (values of csg_status).
@@ -48,23 +51,36 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err);
 // Device layout (all arrays 16-byte aligned, one cudaMalloc):
 //   topo[n]    int4   {left, right, parent, type} for operators,
 //                     {prim, -1, parent, type} for leaves
-//   kids[4n]   float4 for an operator node: its two children's boxes with the child's
-//                     type and primitive index in .w (as int bits):
-//                     {l.min.xyz, l.type} {l.max.xyz, l.prim} {r.min.xyz, r.type} {r.max.xyz, r.prim}
-//                     (the Ulyanov layout: everything GoTo needs at a node in four
-//                     independent 16-byte loads)
+//   kids[5n]   for an operator node, everything GoTo needs in five independent 16-byte
+//                     loads (the Ulyanov layout): the two children's boxes with the
+//                     child's type and primitive index in .w (as int bits), then the
+//                     children's leaf ranges:
+//                     {l.min.xyz, l.type} {l.max.xyz, l.prim} {r.min.xyz, r.type}
+//                     {r.max.xyz, r.prim} {l.leaf_lo, l.leaf_hi, r.leaf_lo, r.leaf_hi}
 //   geo[2p]    float4 {cx, cy, cz, p0} {p1, p2, p3, p4}
 //   color[p]   float4 {r, g, b, 0}
+//   bvh[4b]    a binary BVH over the leaves' own boxes (the reference's boxes), used
+//                     only to find the primitives a ray can hit; per node the two
+//                     children's boxes: {min.xyz, child} {max.xyz, type} x 2, where
+//                     child >= 0 is a BVH node and child < 0 is leaf ~prim (type valid)
 // ---------------------------------------------------------------------------------
+constexpr int kKidsPerNode = 5;
+constexpr int kLiveWordsMax = 32;  // live-leaf mask: at most 32 words (1024 bits) per ray
+
 struct DeviceScene {
     const int4* topo = nullptr;
     const float4* kids = nullptr;
     const float4* geo = nullptr;
     const float4* color = nullptr;
+    const float4* bvh = nullptr;
     int32_t n_nodes = 0;
     int32_t n_prims = 0;
     int32_t op_depth = 0;
     int32_t stack_class = 0;
+    int32_t n_bvh = 0;        // BVH nodes (0: a single primitive, no BVH)
+    int32_t live_words = 0;   // words of the per-ray live mask
+    int32_t live_shift = 0;   // log2 of the leaves per live bit
+    int32_t prepass = 0;      // run the liveness pre-pass (scenes with enough leaves)
 };
 
 // Host image of the device arrays (for upload and for tests).
@@ -73,6 +89,9 @@ struct PackedScene {
     std::vector<float4> kids;
     std::vector<float4> geo;
     std::vector<float4> color;
+    std::vector<float4> bvh;
+    int32_t live_words = 0;
+    int32_t live_shift = 0;
 };
 void pack_scene(const HostTree& tree, PackedScene& out);
 
@@ -82,5 +101,9 @@ void pack_scene(const HostTree& tree, PackedScene& out);
 // reaches the reference's 32-entry limit (RaycastingKernels.cuh:19).  Deeper trees use
 // the 32-entry class, which reproduces the reference's drop-on-full behaviour.
 int32_t stack_class_for_depth(int32_t op_depth);
+
+// Whether renders of a scene with this many primitives run the liveness pre-pass (for a
+// handful of primitives the pre-pass costs more than the pruning saves).
+bool use_prepass(int32_t n_prims);
 
 }  // namespace csgrt

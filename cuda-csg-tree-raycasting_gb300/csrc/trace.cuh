@@ -91,6 +91,27 @@ __device__ __forceinline__ V3 normalize3(V3 a)
     return scale3(inv, a);
 }
 
+// Natural-form helpers: plain operators, contracted by nvcc's default --fmad=true the
+// way it contracts the same expressions in the reference source (Float3Utils.cuh).
+// Used where the contraction of the reference kernel depends on how the compiler shares
+// products between expressions (the cylinder test and the shading).
+namespace nat {
+__device__ __forceinline__ V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 neg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ V3 scale(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 at(V3 o, V3 d, float t)
+{
+    const V3 td = scale(t, d);
+    return V3{o.x + td.x, o.y + td.y, o.z + td.z};
+}
+__device__ __forceinline__ V3 normalize(V3 a)
+{
+    const float inv = 1.0f / sqrtf(dot(a, a));
+    return scale(inv, a);
+}
+}  // namespace nat
+
 // RayHitMinimal (Ray.cuh:36-52) held in registers.
 struct Hit {
     float t;
@@ -110,7 +131,17 @@ __device__ __forceinline__ Hit unpack_hit(float t, uint32_t b)
 
 struct Ray {
     V3 o, d;
+    V3 inv;      // rn(1/d) per component, for the certified box test
+    bool exact;  // a direction component is subnormal: box tests use divisions only
 };
+
+__device__ __forceinline__ void ray_finish(Ray& r)
+{
+    r.inv = V3{__frcp_rn(r.d.x), __frcp_rn(r.d.y), __frcp_rn(r.d.z)};
+    constexpr float kMinNormal = 1.1754943508222875e-38f;
+    auto sub = [](float v) { return v != 0.0f && fabsf(v) < kMinNormal; };
+    r.exact = sub(r.d.x) || sub(r.d.y) || sub(r.d.z);
+}
 
 // RaycastKernel ray generation (RaycastingKernels.cu:11-27) + the Ray constructor's
 // second normalisation (Ray.cuh:12-18).  width/height are floats, as in the reference.
@@ -130,12 +161,13 @@ __device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float
     Ray r;
     r.o = mk(cam[0], cam[1], cam[2]);
     r.d = mk(__fmul_rn(d.x, inv), __fmul_rn(d.y, inv), __fmul_rn(d.z, inv));
+    ray_finish(r);
     return r;
 }
 
 // isBVHNodeHit (RaycastingKernels.cu:718-756): slab test with six divisions.
-// Returns true when the box must be entered; a cull sets hit = Miss and keeps t, idx.
-__device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, float tmin)
+// Returns true when the box must be entered (a cull sets hit = Miss in the caller).
+__device__ __forceinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
 {
     const float t1 = __fdiv_rn(__fsub_rn(lo.x, r.o.x), r.d.x);
     const float t2 = __fdiv_rn(__fsub_rn(hi.x, r.o.x), r.d.x);
@@ -149,6 +181,39 @@ __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, floa
     if (tmn > tmx) return false;
     if (tmn <= tmin && tmx <= tmin) return false;
     return true;
+}
+
+// The same decision from per-ray reciprocals, certified.  With s = b - o rounded as in
+// the reference, t' = rn(s * rn(1/d)) and t = rn(s / d) differ by at most 3u|t|
+// (u = 2^-24).  x -> x -+ 3u|x| are increasing maps and min/max commute with increasing
+// maps, so the reciprocal tmn' and tmx' are each within 3u of the reference's tmn and
+// tmx in the same relative sense.  The sign of tmx is therefore exact, and the two other
+// comparisons (tmn > tmx, tmx <= tmin) are exact whenever the operands differ by more
+// than 2^-20 of their magnitude (a 5x margin over the bound, covering the rounding of the
+// margin test itself).  Anything closer, and anything infinite, tiny or NaN, is decided
+// again with divisions; a ray with a subnormal direction component (whose reciprocal
+// overflows) always uses divisions (Ray::exact).
+__device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, float tmin)
+{
+    if (r.exact) return box_hit_exact(r, lo, hi, tmin);
+    const float t1 = __fmul_rn(__fsub_rn(lo.x, r.o.x), r.inv.x);
+    const float t2 = __fmul_rn(__fsub_rn(hi.x, r.o.x), r.inv.x);
+    const float t3 = __fmul_rn(__fsub_rn(lo.y, r.o.y), r.inv.y);
+    const float t4 = __fmul_rn(__fsub_rn(hi.y, r.o.y), r.inv.y);
+    const float t5 = __fmul_rn(__fsub_rn(lo.z, r.o.z), r.inv.z);
+    const float t6 = __fmul_rn(__fsub_rn(hi.z, r.o.z), r.inv.z);
+    const float tmn = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+    const float tmx = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
+    const float an = fabsf(tmn), ax = fabsf(tmx);
+    constexpr float kRel = 9.5367431640625e-07f;     // 2^-20
+    constexpr float kTiny = 7.888609052210118e-31f;  // 2^-100
+    const bool sure = (fabsf(__fsub_rn(tmn, tmx)) > kRel * (an + ax)) &&
+                      (fabsf(__fsub_rn(tmx, tmin)) > kRel * ax) && (an > kTiny) && (ax > kTiny) &&
+                      (ax < 3.0e38f) && (an < 3.0e38f);
+    if (!sure) return box_hit_exact(r, lo, hi, tmin);
+    if (tmx < 0.0f) return false;
+    if (tmn > tmx) return false;
+    return tmx > tmin;
 }
 
 // sphereHit (RaycastingKernels.cu:135-181)
@@ -205,6 +270,75 @@ __device__ __forceinline__ void cylinder_caps(const Ray& r, V3 V, V3 OC, V3 cen,
     }
 }
 
+#ifndef CSG_CYLINDER_EXPLICIT
+// cylinderHit (RaycastingKernels.cu:202-336), natural form.
+__device__ __forceinline__ void cylinder_caps_n(const Ray& r, V3 V, V3 OC, V3 cen, float hgt, float m,
+                                                float& temp, bool& skip, int& use)
+{
+    if (m < 0.0f) {
+        const float den = nat::dot(r.d, nat::neg(V));
+        if (fabsf(den) < 0.0001f) {
+            skip = true;
+        } else {
+            temp = nat::dot(nat::neg(OC), nat::neg(V)) / den;
+            use = 1;
+        }
+    }
+    if (m > hgt) {
+        const float den = nat::dot(r.d, V);
+        if (fabsf(den) < 0.0001f) {
+            skip = true;
+        } else {
+            const V3 ocm = nat::sub(nat::sub(r.o, cen), nat::scale(hgt / 2, V));
+            temp = nat::dot(nat::neg(ocm), V) / den;
+            use = 2;
+        }
+    }
+}
+
+__device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1, int32_t id, Hit& h,
+                                             float tmin)
+{
+    h.hit = kMiss;
+    h.idx = id;
+    const float rad = g0.w, hgt = g1.x;
+    const V3 V = mk(g1.y, g1.z, g1.w);
+    const V3 cen = mk(g0.x, g0.y, g0.z);
+    const V3 C = nat::sub(cen, nat::scale(hgt / 2, V));
+    const V3 OC = nat::sub(r.o, C);
+    const float aHelp = nat::dot(r.d, V);
+    const float a = fmaxf(1 - aHelp * aHelp, 0.00001f);
+    const float cHelp = nat::dot(OC, V);
+    const float c = nat::dot(OC, OC) - cHelp * cHelp - rad * rad;
+    const float b = (nat::dot(r.d, OC) - nat::dot(r.d, V) * nat::dot(OC, V));
+    const float disc = b * b - a * c;
+    if (disc < 0.0f) return;
+    const float t1 = (-b - sqrtf(disc)) / (a), t2 = (-b + sqrtf(disc)) / (a);
+    const float m1 = t1 * nat::dot(r.d, V) + nat::dot(OC, V), m2 = t2 * nat::dot(r.d, V) + nat::dot(OC, V);
+    if ((m1 < 0.0f && m2 < 0.0f) || (m1 > hgt && m2 > hgt)) return;
+    float temp = t1, m = m1;
+    bool skip = false;
+    int use = 0;
+    cylinder_caps_n(r, V, OC, cen, hgt, m, temp, skip, use);
+    if (temp <= tmin || skip) {
+        temp = t2;
+        m = m2;
+        skip = false;
+        use = 0;
+        cylinder_caps_n(r, V, OC, cen, hgt, m, temp, skip, use);
+        if (temp <= tmin || skip) return;
+    }
+    h.t = temp;
+    V3 n;
+    if (use == 1) n = nat::neg(V);
+    else if (use == 2) n = V;
+    else n = nat::sub(nat::sub(nat::at(r.o, r.d, temp), C), nat::scale(m, V));
+    h.hit = (nat::dot(n, r.d) <= 0.0f) ? kEnter : kExit;
+    if (use == 1) h.hit |= kFlag1;
+    else if (use == 2) h.hit |= kFlag2;
+    h.type = kCylinder;
+}
+#else
 // cylinderHit (RaycastingKernels.cu:202-336)
 __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1, int32_t id, Hit& h,
                                              float tmin)
@@ -252,6 +386,7 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     else if (use == 2) h.hit |= kFlag2;
     h.type = kCylinder;
 }
+#endif
 
 // cubeHit (RaycastingKernels.cu:375-434): axis-aligned slab test.
 __device__ __forceinline__ void cube_hit(const Ray& r, float4 g0, int32_t id, Hit& h, float tmin)
@@ -360,144 +495,373 @@ struct SmemStacks {
     }
 };
 
-// CSGRayCast (RaycastingKernels.cu:459-512) with GoTo (:514-595), Compute (:597-661),
-// LookUpActions (:664-706) and GetParent (:708-716).  `tab` is the 27-entry table in
-// shared memory.  Returns the final hit; *iters receives the loop count (kIterCap+1 if
-// the ray was stopped).
+// Per-ray live-leaf mask.  Bit g stands for leaves [g << shift, (g + 1) << shift); a
+// clear bit means every leaf of the group is known to return Miss for every tmin the
+// traversal can still use.  That is sound because a leaf's result is monotone in tmin
+// (a Miss stays a Miss when tmin grows: a sphere needs a root beyond tmin, a cylinder a
+// valid branch beyond tmin, a box tmx beyond tmin), and the tmin with which the traversal
+// reaches any node never decreases (loops only move tmin forward, SaveLft restores the
+// tmin the parent was entered with).  A subtree whose leaves are all Miss evaluates to a
+// Miss whether or not it is traversed, and a Miss's t and index reach no decision and no
+// output, so skipping such a subtree changes nothing.  Bits are cleared when a leaf test
+// returns Miss and when an operator child's box culls (its leaves' boxes are nested in
+// it, so they cull too).  The mask lives in shared memory, word k of a lane at
+// w[k * nt]; `sum` has bit k set while word k is non-zero.
+struct LiveMask {
+    uint32_t* w;
+    int nt;
+    int shift;
+    int words;
+    uint32_t sum;
+
+    __device__ __forceinline__ uint32_t& word(int k) { return w[k * nt]; }
+    __device__ __forceinline__ void fill(int n_groups)
+    {
+        sum = 0;
+        for (int k = 0; k < words; ++k) {
+            const int rem = n_groups - 32 * k;
+            const uint32_t v = rem >= 32 ? 0xffffffffu : (rem <= 0 ? 0u : ((1u << rem) - 1u));
+            word(k) = v;
+            if (v) sum |= 1u << k;
+        }
+    }
+    __device__ __forceinline__ void clear_all()
+    {
+        for (int k = 0; k < words; ++k) word(k) = 0u;
+        sum = 0;
+    }
+    __device__ __forceinline__ void set_leaf(int leaf)
+    {
+        const int g = leaf >> shift;
+        word(g >> 5) |= 1u << (g & 31);
+        sum |= 1u << (g >> 5);
+    }
+    __device__ __forceinline__ bool any(int lo, int hi)
+    {
+        const int a = lo >> shift, b = hi >> shift;
+        const int wa = a >> 5, wb = b >> 5;
+        const uint32_t ma = 0xffffffffu << (a & 31);
+        const uint32_t mb = 0xffffffffu >> (31 - (b & 31));
+        if (wa == wb) return ((sum >> wa) & 1u) && (word(wa) & ma & mb);
+        const uint32_t mid = (uint32_t)(((1ull << wb) - 1ull) & ~((1ull << (wa + 1)) - 1ull));
+        if (sum & mid) return true;
+        if (((sum >> wa) & 1u) && (word(wa) & ma)) return true;
+        return ((sum >> wb) & 1u) && (word(wb) & mb);
+    }
+    __device__ __forceinline__ void clear_word(int k, uint32_t m)
+    {
+        const uint32_t v = word(k) & ~m;
+        word(k) = v;
+        if (!v) sum &= ~(1u << k);
+    }
+    __device__ __forceinline__ void clear_leaf(int leaf)
+    {
+        if (shift == 0) clear_word(leaf >> 5, 1u << (leaf & 31));
+    }
+    // Clears the groups lying entirely inside [lo, hi].
+    __device__ __forceinline__ void clear_range(int lo, int hi)
+    {
+        const int ga = (lo + (1 << shift) - 1) >> shift, gb = ((hi + 1) >> shift) - 1;
+        if (ga > gb) return;
+        const int wa = ga >> 5, wb = gb >> 5;
+        for (int k = wa; k <= wb; ++k) {
+            if (!((sum >> k) & 1u)) continue;
+            const uint32_t lo_m = (k == wa) ? (0xffffffffu << (ga & 31)) : 0xffffffffu;
+            const uint32_t hi_m = (k == wb) ? (0xffffffffu >> (31 - (gb & 31))) : 0xffffffffu;
+            clear_word(k, lo_m & hi_m);
+        }
+    }
+};
+
+constexpr int kWarpStack = 64;
+
+// Liveness at tmin = 0 of one leaf whose own box already passed at tmin = 0: a cube's box
+// is the cube (the cube test is the same slab test), so it is live; a sphere or cylinder
+// is live when its primitive test at tmin = 0 is not a Miss.
+__device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* __restrict__ geo, int prim,
+                                                  int type)
+{
+    if (type == kCube) return true;
+    Hit h = hit_default();
+    const float4 g0 = __ldg(&geo[2 * prim]);
+    if (type == kSphere) {
+        sphere_hit(ray, g0, prim, h, 0.0f);
+    } else {
+        const float4 g1 = __ldg(&geo[2 * prim + 1]);
+        cylinder_hit(ray, g0, g1, prim, h, 0.0f);
+    }
+    return h.hit != kMiss;
+}
+
+// Liveness pre-pass: the warp walks the BVH over the leaves' own boxes together (its 32
+// rays are an 8x4 pixel tile, so they share most of the walk), each lane testing its own
+// ray, and every lane sets the bits of the leaves whose box passes at tmin = 0 and whose
+// primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
+// active == false only follow.  If the walk would overflow the warp's stack, every lane
+// falls back to an all-live mask (the traversal then decides everything itself).
+__device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LiveMask& lm,
+                                             int* wstack)
+{
+    const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
+    if (!sc.prepass || sc.n_bvh == 0) {
+        lm.fill(n_groups);
+        return;
+    }
+    lm.clear_all();
+    const float4* __restrict__ bvh = sc.bvh;
+    int node = 0, sp = 0;
+    bool overflow = false;
+    while (true) {
+        const float4 a0 = __ldg(&bvh[4 * node + 0]);
+        const float4 a1 = __ldg(&bvh[4 * node + 1]);
+        const float4 a2 = __ldg(&bvh[4 * node + 2]);
+        const float4 a3 = __ldg(&bvh[4 * node + 3]);
+        const int cl = __float_as_int(a0.w), cr = __float_as_int(a2.w);
+        const bool hl = active && box_hit(ray, a0, a1, 0.0f);
+        const bool hr = active && box_hit(ray, a2, a3, 0.0f);
+        if (hl && cl < 0 && leaf_live_at_zero(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
+        if (hr && cr < 0 && leaf_live_at_zero(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
+        const bool dl = __any_sync(0xffffffffu, hl && cl >= 0);
+        const bool dr = __any_sync(0xffffffffu, hr && cr >= 0);
+        if (dl && dr) {
+            if (sp >= kWarpStack) {
+                overflow = true;
+                break;
+            }
+            wstack[sp] = cr;  // every lane writes the same value
+            ++sp;
+            node = cl;
+        } else if (dl) {
+            node = cl;
+        } else if (dr) {
+            node = cr;
+        } else {
+            if (sp == 0) break;
+            __syncwarp();
+            node = wstack[--sp];
+        }
+        __syncwarp();
+    }
+    if (overflow) lm.fill(n_groups);
+}
+
+// One child of an operator node during GoTo (RaycastingKernels.cu:540-553): the box
+// test of isBVHNodeHit and, for a leaf that passes it, the primitive test.  Returns true
+// when the traversal must descend into the child.
+//
+// The primitive test of a leaf is a function of the ray, the primitive and tmin only, and
+// a Miss's t and index never reach a decision or an output (every table cell that
+// compares t or loops on t has both sides, or the looping side, non-Miss), so for leaves
+// the order of the two tests can change without changing any result:
+//  * cube: its box is the cube itself, and cubeHit repeats the identical slab test, so the
+//    box test is implied and skipped;
+//  * sphere: the sphere test runs first; only a hit is confirmed with the box test;
+//  * cylinder: its box is not conservative (BVHNode.cuh:34-49) and does cut hits, so the
+//    box test runs first, as in the reference.
+__device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restrict__ geo, float4 lo, float4 hi,
+                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LiveMask& lm)
+{
+    if (!lm.any(leaf_lo, leaf_hi)) {
+        H.hit = kMiss;
+        return false;
+    }
+    const int32_t prim = __float_as_int(hi.w);
+    if (prim < 0) {
+        const bool go = box_hit(ray, lo, hi, tmin);
+        if (!go) {
+            H.hit = kMiss;
+            lm.clear_range(leaf_lo, leaf_hi);
+        }
+        return go;
+    }
+    const int32_t type = __float_as_int(lo.w);
+    const float4 g0 = __ldg(&geo[2 * prim]);
+    if (type == kSphere) {
+        sphere_hit(ray, g0, prim, H, tmin);
+        if (H.hit != kMiss && !box_hit(ray, lo, hi, tmin)) H.hit = kMiss;
+    } else if (type == kCube) {
+        cube_hit(ray, g0, prim, H, tmin);
+    } else {
+        if (box_hit(ray, lo, hi, tmin)) {
+            const float4 g1 = __ldg(&geo[2 * prim + 1]);
+            cylinder_hit(ray, g0, g1, prim, H, tmin);
+        } else {
+            H.hit = kMiss;
+        }
+    }
+    if (H.hit == kMiss) lm.clear_leaf(prim);
+    return false;
+}
+
+// Per-ray traversal state of CSGRayCast (RaycastingKernels.cu:459-512), advanced one loop
+// iteration at a time by step() so that a lane can finish its ray and take another
+// while the rest of its warp is still traversing.
+struct Tracer {
+    Ray ray;
+    Hit L, R;
+    float tmin;
+    int32_t cur;
+    int4 ct;          // topology of `cur`; the virtual node CSGNode(0,0,0,0,0) is {0,0,0,Union}
+    uint32_t action;
+    ActionStack as;
+    int32_t np, ntm;  // primitive / time stack depths (entries in shared memory)
+    uint32_t it;
+    bool run;
+
+    __device__ __forceinline__ bool busy() const { return run || as.n > 0; }
+};
+
 template <int SD>
-__device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, SmemStacks<SD>& st,
-                                            const uint16_t* tab, uint32_t iter_cap, uint32_t* iters)
+__device__ __forceinline__ void tracer_begin(Tracer& T, SmemStacks<SD>& st)
+{
+    T.as = ActionStack{0ull, 0};
+    T.np = 0;
+    T.ntm = 0;
+    // Slot 0 of the primitive and time stacks is what a pop from an empty stack returns.
+    st.pt[st.tid] = -1.0f;
+    st.pb[st.tid] = kMiss | (0xffffu << 16);
+    st.tt[st.tid] = 0.0f;
+    T.tmin = 0.0f;
+    T.cur = -1;
+    T.ct = make_int4(0, 0, 0, kUnion);
+    T.L = hit_default();
+    T.R = hit_default();
+    T.as.push(kCompute);
+    T.action = kGotoL;
+    T.run = true;
+    T.it = 0;
+}
+
+// GetParent (RaycastingKernels.cu:708-716)
+__device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict__ topo)
+{
+    if (T.ct.z >= 0) {
+        T.cur = T.ct.z;
+        T.ct = __ldg(&topo[T.cur]);
+    } else {
+        T.run = false;
+        T.cur = -1;
+        T.ct = make_int4(0, 0, 0, kUnion);
+    }
+}
+
+// One iteration of the CSGRayCast loop: SaveLft, GoTo (:514-595), Compute (:597-661) with
+// LookUpActions (:664-706).  `tab` is the 27-entry table in shared memory.
+template <int SD>
+__device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, SmemStacks<SD>& st,
+                                            const uint16_t* tab, LiveMask& lm)
 {
     const int4* __restrict__ topo = sc.topo;
     const float4* __restrict__ kids = sc.kids;
     const float4* __restrict__ geo = sc.geo;
-
-    ActionStack as{0ull, 0};
-    st.np = 0;
-    st.ntm = 0;
-    // Slot 0 of the primitive and time stacks is what an empty pop returns.
-    st.pt[st.tid] = -1.0f;
-    st.pb[st.tid] = kMiss | (0xffffu << 16);
-    st.tt[st.tid] = 0.0f;
-
-    float tmin = 0.0f;
-    int cur = -1;
-    int4 ct = make_int4(0, 0, 0, kUnion);  // the virtual node CSGNode(0,0,0,0,0)
-    Hit L = hit_default(), R = hit_default();
-    as.push(kCompute);
-    uint32_t action = kGotoL;
-    bool run = true;
-    uint32_t it = 0;
-
-    auto parent = [&]() {
-        if (ct.z >= 0) {
-            cur = ct.z;
-            ct = __ldg(&topo[cur]);
-        } else {
-            run = false;
-            cur = -1;
-            ct = make_int4(0, 0, 0, kUnion);
-        }
-    };
-
-    while (run || as.n > 0) {
-        if (++it > iter_cap) {
-            *iters = it;
-            return hit_default();
-        }
-        if (action & kSaveL) {
-            tmin = st.tpop();
-            st.ppush(L);
-            action = kGotoR;
-        }
-        if (action & (kGotoL | kGotoR)) {
-            cur = (action & kGotoL) ? ct.x : ct.y;
-            ct = __ldg(&topo[cur]);
-            if (ct.w <= kIntersection) {
-                const float4 k0 = __ldg(&kids[4 * cur + 0]);
-                const float4 k1 = __ldg(&kids[4 * cur + 1]);
-                const float4 k2 = __ldg(&kids[4 * cur + 2]);
-                const float4 k3 = __ldg(&kids[4 * cur + 3]);
-                bool gl = box_hit(ray, k0, k1, tmin);
-                bool gr = box_hit(ray, k2, k3, tmin);
-                if (!gl) L.hit = kMiss;
-                if (!gr) R.hit = kMiss;
-                const int32_t lprim = __float_as_int(k1.w), rprim = __float_as_int(k3.w);
-                if (gl && lprim != -1) {
-                    hit_primitive(ray, geo, __float_as_int(k0.w), lprim, L, tmin);
-                    gl = false;
-                }
-                if (gr && rprim != -1) {
-                    hit_primitive(ray, geo, __float_as_int(k2.w), rprim, R, tmin);
-                    gr = false;
-                }
-                if (gl || gr) {
-                    if (!gl) {
-                        st.ppush(L);
-                        as.push(kLoadL);
-                        action = kGotoR;
-                    } else if (!gr) {
-                        st.ppush(R);
-                        as.push(kLoadR);
-                        action = kGotoL;
-                    } else {
-                        st.tpush(tmin);
-                        as.push(kLoadL);
-                        as.push(kSaveL);
-                        action = kGotoL;
-                    }
+    ++T.it;
+    st.np = T.np;
+    st.ntm = T.ntm;
+    if (T.action & kSaveL) {
+        T.tmin = st.tpop();
+        st.ppush(T.L);
+        T.action = kGotoR;
+    }
+    if (T.action & (kGotoL | kGotoR)) {
+        T.cur = (T.action & kGotoL) ? T.ct.x : T.ct.y;
+        T.ct = __ldg(&topo[T.cur]);
+        if (T.ct.w <= kIntersection) {
+            const float4* kn = &kids[kKidsPerNode * T.cur];
+            const float4 k0 = __ldg(&kn[0]);
+            const float4 k1 = __ldg(&kn[1]);
+            const float4 k2 = __ldg(&kn[2]);
+            const float4 k3 = __ldg(&kn[3]);
+            const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
+            const bool gl = child_test(T.ray, geo, k0, k1, rg.x, rg.y, T.L, T.tmin, lm);
+            const bool gr = child_test(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
+            if (gl || gr) {
+                if (!gl) {
+                    st.ppush(T.L);
+                    T.as.push(kLoadL);
+                    T.action = kGotoR;
+                } else if (!gr) {
+                    st.ppush(T.R);
+                    T.as.push(kLoadR);
+                    T.action = kGotoL;
                 } else {
-                    action = kCompute;
+                    st.tpush(T.tmin);
+                    T.as.push(kLoadL);
+                    T.as.push(kSaveL);
+                    T.action = kGotoL;
                 }
             } else {
-                if (action & kGotoL) hit_primitive(ray, geo, ct.w, ct.x, L, tmin);
-                else hit_primitive(ray, geo, ct.w, ct.x, R, tmin);
-                action = as.pop();
-                parent();
+                T.action = kCompute;
             }
-        }
-        if (action & (kLoadL | kLoadR | kCompute)) {
-            if (action & kLoadL) L = st.ppop();
-            else if (action & kLoadR) R = st.ppop();
-            // LookUpActions: Enter -> 0, Exit -> 1, Miss -> 2, tested in that order.
-            uint32_t li = L.hit, ri = R.hit;
-            li = (li & kEnter) ? 0u : li;
-            li = (li & kExit) ? 1u : li;
-            li = (li & kMiss) ? 2u : li;
-            ri = (ri & kEnter) ? 0u : ri;
-            ri = (ri & kExit) ? 1u : ri;
-            ri = (ri & kMiss) ? 2u : ri;
-            const uint32_t op = (uint32_t)ct.w;
-            const uint32_t acts = (op <= 2u && li <= 2u && ri <= 2u) ? tab[op * 9 + li * 3 + ri] : 0xffffffffu;
-            if ((acts & hRetL) || ((acts & hRetLC) && (L.t < R.t))) {
-                R = L;
-                action = as.pop();
-                parent();
-            } else if ((acts & hRetR) || ((acts & hRetRC) && (L.t > R.t))) {
-                if (acts & hFlipR) R.hit ^= (kFlip | kExit | kEnter);
-                L = R;
-                action = as.pop();
-                parent();
-            } else if ((acts & hLoopL) || ((acts & hLoopLC) && (L.t < R.t))) {
-                tmin = L.t;
-                st.ppush(R);
-                as.push(kLoadR);
-                action = kGotoL;
-            } else if ((acts & hLoopR) || ((acts & hLoopRC) && (L.t > R.t))) {
-                tmin = R.t;
-                st.ppush(L);
-                as.push(kLoadL);
-                action = kGotoR;
-            } else {
-                R = hit_default();
-                L = hit_default();
-                action = as.pop();
-                parent();
-            }
+        } else {
+            Hit& H = (T.action & kGotoL) ? T.L : T.R;
+            hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
+            if (H.hit == kMiss) lm.clear_leaf(T.ct.x);
+            T.action = T.as.pop();
+            tracer_parent(T, topo);
         }
     }
-    *iters = it;
-    return L;
+    if (T.action & (kLoadL | kLoadR | kCompute)) {
+        if (T.action & kLoadL) T.L = st.ppop();
+        else if (T.action & kLoadR) T.R = st.ppop();
+        // LookUpActions: Enter -> 0, Exit -> 1, Miss -> 2, tested in that order.
+        uint32_t li = T.L.hit, ri = T.R.hit;
+        li = (li & kEnter) ? 0u : li;
+        li = (li & kExit) ? 1u : li;
+        li = (li & kMiss) ? 2u : li;
+        ri = (ri & kEnter) ? 0u : ri;
+        ri = (ri & kExit) ? 1u : ri;
+        ri = (ri & kMiss) ? 2u : ri;
+        const uint32_t op = (uint32_t)T.ct.w;
+        const uint32_t acts = (op <= 2u && li <= 2u && ri <= 2u) ? tab[op * 9 + li * 3 + ri] : 0xffffffffu;
+        const bool lt = T.L.t < T.R.t, gt = T.L.t > T.R.t;
+        if ((acts & hRetL) || ((acts & hRetLC) && lt)) {
+            T.R = T.L;
+            T.action = T.as.pop();
+            tracer_parent(T, topo);
+        } else if ((acts & hRetR) || ((acts & hRetRC) && gt)) {
+            if (acts & hFlipR) T.R.hit ^= (kFlip | kExit | kEnter);
+            T.L = T.R;
+            T.action = T.as.pop();
+            tracer_parent(T, topo);
+        } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
+            T.tmin = T.L.t;
+            st.ppush(T.R);
+            T.as.push(kLoadR);
+            T.action = kGotoL;
+        } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
+            T.tmin = T.R.t;
+            st.ppush(T.L);
+            T.as.push(kLoadL);
+            T.action = kGotoR;
+        } else {
+            T.R = hit_default();
+            T.L = hit_default();
+            T.action = T.as.pop();
+            tracer_parent(T, topo);
+        }
+    }
+    T.np = st.np;
+    T.ntm = st.ntm;
+}
+
+// Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
+// stopped at iter_cap; *capped is then set).
+template <int SD>
+__device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, SmemStacks<SD>& st,
+                                            const uint16_t* tab, LiveMask& lm, uint32_t iter_cap, bool* capped)
+{
+    Tracer T;
+    T.ray = ray;
+    tracer_begin<SD>(T, st);
+    while (T.busy()) {
+        if (T.it >= iter_cap) {
+            *capped = true;
+            return hit_default();
+        }
+        tracer_step<SD>(T, sc, st, tab, lm);
+    }
+    *capped = false;
+    return T.L;
 }
 
 // Hit details (sphere/cylinder/cubeHitDetails, RaycastingKernels.cu:183-200, 338-373,
@@ -513,6 +877,18 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     } else if (h.type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * h.idx + 1]);
         const V3 V = mk(g1.y, g1.z, g1.w);
+#ifndef CSG_CYLINDER_EXPLICIT
+        const V3 C = nat::sub(cen, nat::scale(g1.x / 2, V));
+        const V3 OC = nat::sub(ray.o, C);
+        if (h.hit & kFlag1) {
+            N = neg3(V);
+        } else if (h.hit & kFlag2) {
+            N = V;
+        } else {
+            const float m = nat::dot(ray.d, V) * h.t + nat::dot(OC, V);
+            N = nat::normalize(nat::sub(nat::sub(P, C), nat::scale(m, V)));
+        }
+#else
         const V3 C = sub_scaled(cen, __fdiv_rn(g1.x, 2.0f), V);
         const V3 OC = sub3(ray.o, C);
         if (h.hit & kFlag1) {
@@ -523,6 +899,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
             const float m = __fmaf_rn(dot3(ray.d, V), h.t, dot3(OC, V));
             N = normalize3(sub_scaled(sub3(P, C), m, V));
         }
+#endif
     } else {
         const V3 PC = sub3(P, cen);
         const float bias = 1.00001f;  // `float bias = 1.00001;` rounds to the same float
@@ -538,6 +915,27 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
 
 // LightningKernel (RaycastingKernels.cu:62-105): Phong with ka 0.2, kd 0.8, ks 0.7,
 // shininess 30 and a white light; clamped to [0, 1].
+#ifndef CSG_SHADING_EXPLICIT
+__device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, float4 col)
+{
+    const V3 white = mk(1.0f, 1.0f, 1.0f);
+    const float ka = 0.2f, kd = 0.8f, ks = 0.7f, shininess = 30.0f;
+    const V3 L = nat::normalize(light);
+    const V3 Vd = nat::normalize(nat::sub(mk(cam[0], cam[1], cam[2]), P));
+    const V3 nL = nat::neg(L);
+    const V3 nn = nat::normalize(N);
+    const V3 Rd = nat::sub(nL, nat::scale(2.0f * (nat::dot(nL, nn)), nn));
+    const V3 ambient = nat::scale(ka, white);
+    const float diff = fmaxf(nat::dot(N, L), 0.0f);
+    const V3 diffuse = nat::scale(kd * diff, white);
+    const float spec = powf(fmaxf(nat::dot(Vd, Rd), 0.0f), shininess);
+    const V3 specular = nat::scale(ks * spec, white);
+    V3 c = mk(col.x * (ambient.x + diffuse.x + specular.x), col.y * (ambient.y + diffuse.y + specular.y),
+              col.z * (ambient.z + diffuse.z + specular.z));
+    return make_float4(fminf(fmaxf(c.x, 0.0f), 1.0f), fminf(fmaxf(c.y, 0.0f), 1.0f),
+                       fminf(fmaxf(c.z, 0.0f), 1.0f), 1.0f);
+}
+#else
 __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, float4 col)
 {
     const V3 Ld = normalize3(light);
@@ -552,6 +950,7 @@ __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, 
                        fminf(fmaxf(__fmul_rn(col.y, shade), 0.0f), 1.0f),
                        fminf(fmaxf(__fmul_rn(col.z, shade), 0.0f), 1.0f), 1.0f);
 }
+#endif
 
 __device__ __forceinline__ uint32_t quantize_rgba8(float4 c)
 {

@@ -181,6 +181,7 @@ def make_gpu(out_path: str):
         out = G.render(nodes44, prims48, cam, light, w, h)
         for k, v in planes_from(out, w * h).items():
             arrays[f"{name}/{k}"] = v
+        arrays[f"{name}/rgba_hit"] = out["rgba"][out["hit"] == 1].astype(np.float32)
         arrays[f"{name}/camera"] = cam
         arrays[f"{name}/light"] = np.float32(light)
         arrays[f"{name}/size"] = np.int32([w, h])
