@@ -244,33 +244,28 @@ __device__ __forceinline__ void sphere_hit(const Ray& r, float4 g0, int32_t id, 
     h.type = kSphere;
 }
 
-// Cap-plane step of cylinderHit (RaycastingKernels.cu:238-266 / 273-301).
-__device__ __forceinline__ void cylinder_caps(const Ray& r, V3 V, V3 OC, V3 cen, float h2, float hgt,
-                                              float m, float& temp, bool& skip, int& use)
+// Inside cylinderHit and reflect nvcc shares some products between expressions and leaves
+// those unfused, so some dot products there have other shapes than dot3 (matched against
+// the reference kernel's own intermediates on ~20k cylinder rays and ~37k shaded pixels):
+//   dot(d, V), and the cap denominators dot(d, +-V):  rn(fma(y, y', x*x') + z*z')
+//   the top cap's numerator dot(-(o - c - (h/2)V), V) and reflect's dot(-L, n):
+//                                                    fma(z, z', fma(y, y', x*x'))
+// and c - (h/2)V is a product rounded on its own followed by the subtraction.
+__device__ __forceinline__ float dot_yx_z(V3 a, V3 b)
 {
-    if (m < 0.0f) {
-        const V3 nV = neg3(V);
-        const float den = dot3(r.d, nV);
-        if (fabsf(den) < 0.0001f) {
-            skip = true;
-        } else {
-            temp = __fdiv_rn(dot3(neg3(OC), nV), den);
-            use = 1;
-        }
-    }
-    if (m > hgt) {
-        const float den = dot3(r.d, V);
-        if (fabsf(den) < 0.0001f) {
-            skip = true;
-        } else {
-            const V3 ocm = sub_scaled(sub3(r.o, cen), h2, V);
-            temp = __fdiv_rn(dot3(neg3(ocm), V), den);
-            use = 2;
-        }
-    }
+    return __fadd_rn(__fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ float dot_zyx(V3 a, V3 b)
+{
+    return __fmaf_rn(a.z, b.z, __fmaf_rn(a.y, b.y, __fmul_rn(a.x, b.x)));
+}
+__device__ __forceinline__ V3 sub_scaled_unfused(V3 a, float s, V3 b)
+{
+    return V3{__fsub_rn(a.x, __fmul_rn(s, b.x)), __fsub_rn(a.y, __fmul_rn(s, b.y)),
+              __fsub_rn(a.z, __fmul_rn(s, b.z))};
 }
 
-#ifndef CSG_CYLINDER_EXPLICIT
+#ifdef CSG_CYLINDER_NATURAL
 // cylinderHit (RaycastingKernels.cu:202-336), natural form.
 __device__ __forceinline__ void cylinder_caps_n(const Ray& r, V3 V, V3 OC, V3 cen, float hgt, float m,
                                                 float& temp, bool& skip, int& use)
@@ -339,6 +334,32 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     h.type = kCylinder;
 }
 #else
+// Cap-plane step of cylinderHit (RaycastingKernels.cu:238-266 / 273-301).
+__device__ __forceinline__ void cylinder_caps(const Ray& r, V3 V, V3 OC, V3 cen, float h2, float hgt,
+                                              float m, float& temp, bool& skip, int& use)
+{
+    if (m < 0.0f) {
+        const V3 nV = neg3(V);
+        const float den = dot_yx_z(r.d, nV);
+        if (fabsf(den) < 0.0001f) {
+            skip = true;
+        } else {
+            temp = __fdiv_rn(dot3(neg3(OC), nV), den);
+            use = 1;
+        }
+    }
+    if (m > hgt) {
+        const float den = dot_yx_z(r.d, V);
+        if (fabsf(den) < 0.0001f) {
+            skip = true;
+        } else {
+            const V3 ocm = sub_scaled_unfused(sub3(r.o, cen), h2, V);
+            temp = __fdiv_rn(dot_zyx(neg3(ocm), V), den);
+            use = 2;
+        }
+    }
+}
+
 // cylinderHit (RaycastingKernels.cu:202-336)
 __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1, int32_t id, Hit& h,
                                              float tmin)
@@ -349,9 +370,9 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     const V3 V = mk(g1.y, g1.z, g1.w);
     const V3 cen = mk(g0.x, g0.y, g0.z);
     const float h2 = __fdiv_rn(hgt, 2.0f);
-    const V3 C = sub_scaled(cen, h2, V);
+    const V3 C = sub_scaled_unfused(cen, h2, V);
     const V3 OC = sub3(r.o, C);
-    const float dV = dot3(r.d, V);
+    const float dV = dot_yx_z(r.d, V);
     const float a = fmaxf(__fmaf_rn(-dV, dV, 1.0f), 0.00001f);
     const float cH = dot3(OC, V);
     const float c = __fmaf_rn(-rad, rad, __fmaf_rn(-cH, cH, dot3(OC, OC)));
@@ -877,7 +898,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     } else if (h.type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * h.idx + 1]);
         const V3 V = mk(g1.y, g1.z, g1.w);
-#ifndef CSG_CYLINDER_EXPLICIT
+#ifdef CSG_CYLINDER_NATURAL
         const V3 C = nat::sub(cen, nat::scale(g1.x / 2, V));
         const V3 OC = nat::sub(ray.o, C);
         if (h.hit & kFlag1) {
@@ -915,7 +936,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
 
 // LightningKernel (RaycastingKernels.cu:62-105): Phong with ka 0.2, kd 0.8, ks 0.7,
 // shininess 30 and a white light; clamped to [0, 1].
-#ifndef CSG_SHADING_EXPLICIT
+#ifdef CSG_SHADING_NATURAL
 __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, float4 col)
 {
     const V3 white = mk(1.0f, 1.0f, 1.0f);
@@ -941,8 +962,8 @@ __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, 
     const V3 Ld = normalize3(light);
     const V3 Vd = normalize3(sub3(mk(cam[0], cam[1], cam[2]), P));
     const V3 nL = neg3(Ld);
-    const V3 nn = normalize3(N);  // reflect (Float3Utils.cuh:39-44)
-    const V3 Rd = sub_scaled(nL, __fmul_rn(2.0f, dot3(nL, nn)), nn);
+    const V3 nn = normalize3(N);  // reflect (Float3Utils.cuh:39-44); its dot has the z(y(x)) shape
+    const V3 Rd = sub_scaled(nL, __fmul_rn(2.0f, dot_zyx(nL, nn)), nn);
     const float diff = fmaxf(dot3(N, Ld), 0.0f);
     const float spec = powf(fmaxf(dot3(Vd, Rd), 0.0f), 30.0f);
     const float shade = __fmaf_rn(0.7f, spec, __fmaf_rn(0.8f, diff, 0.2f));

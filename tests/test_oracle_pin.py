@@ -3,9 +3,8 @@
 * "ieee" mode vs the reference kernels compiled for the host (golden fixtures made by
   tests/golden/make_golden.py host): every plane bit-exact.
 * "fma" mode vs the reference kernels compiled by nvcc for sm_103a and run on a GB300
-  (tests/golden/ref_gpu.npz, made by make_golden.py gpu): hit and primitive bit-exact;
-  t and normal bit-exact except on cylinder pixels, where at least 99.5% agree within
-  1e-5 (t relative, unit normal absolute); RGBA8 within 1 LSB (powf differs between the
+  (tests/golden/ref_gpu.npz, made by make_golden.py gpu): hit, primitive, t and normal
+  bit-exact; RGBA8 within 1 LSB and float RGBA within 2e-6 (powf differs between the
   host and device libraries).
 * Live comparison against the host build when the reference sources are present.
 """
@@ -48,18 +47,12 @@ def test_oracle_fma_matches_reference_cuda_kernel(oracle, case):
     assert (out["hit"] == g["hit"]).all()
     m = g["hit"] == 1
     assert (out["prim"][m] == g["prim"][m]).all()
-    # bit-exact except on cylinder pixels, where the oracle's contraction of the quadratic
-    # differs from nvcc's in the last bits: there within 1e-5 relative
-    nodes, _ = oracle.parse(scene_text(case))
-    cyl = np.isin(g["prim"][m], [p for t, p in zip(nodes["type"], nodes["prim"]) if t == 4])
-    assert ulp_equal(out["t"][m][~cyl], g["t"][m][~cyl]).all()
-    assert ulp_equal(out["normal"][m][~cyl], g["normal"][m][~cyl]).all()
-    tc, gc = out["t"][m][cyl], g["t"][m][cyl]
-    nc, gn = out["normal"][m][cyl], g["normal"][m][cyl]
-    ok = (np.abs(tc - gc) <= 1e-5 * np.abs(gc)) & (np.abs(nc - gn).max(1, initial=0) <= 1e-5)
-    assert ok.size == 0 or ok.mean() >= 0.995
+    assert ulp_equal(out["t"][m], g["t"][m]).all()
+    assert ulp_equal(out["normal"][m], g["normal"][m]).all()
     d = np.abs(out["rgba8"].view(np.uint8).astype(int) - g["rgba8"].view(np.uint8).astype(int))
     assert d.max() <= 1
+    if "rgba_hit" in g:
+        assert np.abs(out["rgba"][m] - g["rgba_hit"]).max(initial=0) <= 2e-6
 
 
 def test_oracle_parse_matches_reference_parser(oracle):
