@@ -91,26 +91,6 @@ __device__ __forceinline__ V3 normalize3(V3 a)
     return scale3(inv, a);
 }
 
-// Natural-form helpers: plain operators, contracted by nvcc's default --fmad=true the
-// way it contracts the same expressions in the reference source (Float3Utils.cuh).
-// Used where the contraction of the reference kernel depends on how the compiler shares
-// products between expressions (the cylinder test and the shading).
-namespace nat {
-__device__ __forceinline__ V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
-__device__ __forceinline__ V3 neg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
-__device__ __forceinline__ V3 scale(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
-__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
-__device__ __forceinline__ V3 at(V3 o, V3 d, float t)
-{
-    const V3 td = scale(t, d);
-    return V3{o.x + td.x, o.y + td.y, o.z + td.z};
-}
-__device__ __forceinline__ V3 normalize(V3 a)
-{
-    const float inv = 1.0f / sqrtf(dot(a, a));
-    return scale(inv, a);
-}
-}  // namespace nat
 
 // RayHitMinimal (Ray.cuh:36-52) held in registers.
 struct Hit {
@@ -265,75 +245,6 @@ __device__ __forceinline__ V3 sub_scaled_unfused(V3 a, float s, V3 b)
               __fsub_rn(a.z, __fmul_rn(s, b.z))};
 }
 
-#ifdef CSG_CYLINDER_NATURAL
-// cylinderHit (RaycastingKernels.cu:202-336), natural form.
-__device__ __forceinline__ void cylinder_caps_n(const Ray& r, V3 V, V3 OC, V3 cen, float hgt, float m,
-                                                float& temp, bool& skip, int& use)
-{
-    if (m < 0.0f) {
-        const float den = nat::dot(r.d, nat::neg(V));
-        if (fabsf(den) < 0.0001f) {
-            skip = true;
-        } else {
-            temp = nat::dot(nat::neg(OC), nat::neg(V)) / den;
-            use = 1;
-        }
-    }
-    if (m > hgt) {
-        const float den = nat::dot(r.d, V);
-        if (fabsf(den) < 0.0001f) {
-            skip = true;
-        } else {
-            const V3 ocm = nat::sub(nat::sub(r.o, cen), nat::scale(hgt / 2, V));
-            temp = nat::dot(nat::neg(ocm), V) / den;
-            use = 2;
-        }
-    }
-}
-
-__device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1, int32_t id, Hit& h,
-                                             float tmin)
-{
-    h.hit = kMiss;
-    h.idx = id;
-    const float rad = g0.w, hgt = g1.x;
-    const V3 V = mk(g1.y, g1.z, g1.w);
-    const V3 cen = mk(g0.x, g0.y, g0.z);
-    const V3 C = nat::sub(cen, nat::scale(hgt / 2, V));
-    const V3 OC = nat::sub(r.o, C);
-    const float aHelp = nat::dot(r.d, V);
-    const float a = fmaxf(1 - aHelp * aHelp, 0.00001f);
-    const float cHelp = nat::dot(OC, V);
-    const float c = nat::dot(OC, OC) - cHelp * cHelp - rad * rad;
-    const float b = (nat::dot(r.d, OC) - nat::dot(r.d, V) * nat::dot(OC, V));
-    const float disc = b * b - a * c;
-    if (disc < 0.0f) return;
-    const float t1 = (-b - sqrtf(disc)) / (a), t2 = (-b + sqrtf(disc)) / (a);
-    const float m1 = t1 * nat::dot(r.d, V) + nat::dot(OC, V), m2 = t2 * nat::dot(r.d, V) + nat::dot(OC, V);
-    if ((m1 < 0.0f && m2 < 0.0f) || (m1 > hgt && m2 > hgt)) return;
-    float temp = t1, m = m1;
-    bool skip = false;
-    int use = 0;
-    cylinder_caps_n(r, V, OC, cen, hgt, m, temp, skip, use);
-    if (temp <= tmin || skip) {
-        temp = t2;
-        m = m2;
-        skip = false;
-        use = 0;
-        cylinder_caps_n(r, V, OC, cen, hgt, m, temp, skip, use);
-        if (temp <= tmin || skip) return;
-    }
-    h.t = temp;
-    V3 n;
-    if (use == 1) n = nat::neg(V);
-    else if (use == 2) n = V;
-    else n = nat::sub(nat::sub(nat::at(r.o, r.d, temp), C), nat::scale(m, V));
-    h.hit = (nat::dot(n, r.d) <= 0.0f) ? kEnter : kExit;
-    if (use == 1) h.hit |= kFlag1;
-    else if (use == 2) h.hit |= kFlag2;
-    h.type = kCylinder;
-}
-#else
 // Cap-plane step of cylinderHit (RaycastingKernels.cu:238-266 / 273-301).
 __device__ __forceinline__ void cylinder_caps(const Ray& r, V3 V, V3 OC, V3 cen, float h2, float hgt,
                                               float m, float& temp, bool& skip, int& use)
@@ -407,7 +318,6 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     else if (use == 2) h.hit |= kFlag2;
     h.type = kCylinder;
 }
-#endif
 
 // cubeHit (RaycastingKernels.cu:375-434): axis-aligned slab test.
 __device__ __forceinline__ void cube_hit(const Ray& r, float4 g0, int32_t id, Hit& h, float tmin)
@@ -898,18 +808,6 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     } else if (h.type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * h.idx + 1]);
         const V3 V = mk(g1.y, g1.z, g1.w);
-#ifdef CSG_CYLINDER_NATURAL
-        const V3 C = nat::sub(cen, nat::scale(g1.x / 2, V));
-        const V3 OC = nat::sub(ray.o, C);
-        if (h.hit & kFlag1) {
-            N = neg3(V);
-        } else if (h.hit & kFlag2) {
-            N = V;
-        } else {
-            const float m = nat::dot(ray.d, V) * h.t + nat::dot(OC, V);
-            N = nat::normalize(nat::sub(nat::sub(P, C), nat::scale(m, V)));
-        }
-#else
         const V3 C = sub_scaled(cen, __fdiv_rn(g1.x, 2.0f), V);
         const V3 OC = sub3(ray.o, C);
         if (h.hit & kFlag1) {
@@ -920,7 +818,6 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
             const float m = __fmaf_rn(dot3(ray.d, V), h.t, dot3(OC, V));
             N = normalize3(sub_scaled(sub3(P, C), m, V));
         }
-#endif
     } else {
         const V3 PC = sub3(P, cen);
         const float bias = 1.00001f;  // `float bias = 1.00001;` rounds to the same float
@@ -936,27 +833,6 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
 
 // LightningKernel (RaycastingKernels.cu:62-105): Phong with ka 0.2, kd 0.8, ks 0.7,
 // shininess 30 and a white light; clamped to [0, 1].
-#ifdef CSG_SHADING_NATURAL
-__device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, float4 col)
-{
-    const V3 white = mk(1.0f, 1.0f, 1.0f);
-    const float ka = 0.2f, kd = 0.8f, ks = 0.7f, shininess = 30.0f;
-    const V3 L = nat::normalize(light);
-    const V3 Vd = nat::normalize(nat::sub(mk(cam[0], cam[1], cam[2]), P));
-    const V3 nL = nat::neg(L);
-    const V3 nn = nat::normalize(N);
-    const V3 Rd = nat::sub(nL, nat::scale(2.0f * (nat::dot(nL, nn)), nn));
-    const V3 ambient = nat::scale(ka, white);
-    const float diff = fmaxf(nat::dot(N, L), 0.0f);
-    const V3 diffuse = nat::scale(kd * diff, white);
-    const float spec = powf(fmaxf(nat::dot(Vd, Rd), 0.0f), shininess);
-    const V3 specular = nat::scale(ks * spec, white);
-    V3 c = mk(col.x * (ambient.x + diffuse.x + specular.x), col.y * (ambient.y + diffuse.y + specular.y),
-              col.z * (ambient.z + diffuse.z + specular.z));
-    return make_float4(fminf(fmaxf(c.x, 0.0f), 1.0f), fminf(fmaxf(c.y, 0.0f), 1.0f),
-                       fminf(fmaxf(c.z, 0.0f), 1.0f), 1.0f);
-}
-#else
 __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, float4 col)
 {
     const V3 Ld = normalize3(light);
@@ -971,7 +847,6 @@ __device__ __forceinline__ float4 phong(const float* cam, V3 light, V3 P, V3 N, 
                        fminf(fmaxf(__fmul_rn(col.y, shade), 0.0f), 1.0f),
                        fminf(fmaxf(__fmul_rn(col.z, shade), 0.0f), 1.0f), 1.0f);
 }
-#endif
 
 __device__ __forceinline__ uint32_t quantize_rgba8(float4 c)
 {

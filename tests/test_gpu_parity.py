@@ -77,10 +77,6 @@ def assert_bit_exact(a, b, name, rgba_lsb=1):
         assert d.max() <= rgba_lsb, f"{name}: RGBA8 differs by {d.max()} LSB"
 
 
-def cylinder_prims(nodes) -> set:
-    return {int(p) for t, p in zip(nodes["type"], nodes["prim"]) if t == 4}
-
-
 @pytest.mark.parametrize("case", sorted(HOST_CASES))
 def test_engine_matches_oracle_on_golden_cases(csg, oracle, torch_cuda, case):
     g = HOST_CASES[case]
