@@ -35,7 +35,11 @@ def _sources(names):
     return [CSRC / n for n in names if (CSRC / n).exists()]
 
 
-def build(verbose: bool = False, extra_nvcc: list[str] | None = None) -> str:
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None, out_dir: Path | None = None) -> str:
+    """Builds libcsgrt.so into `out_dir` (default _build/); `extra_nvcc` adds flags to the
+    CUDA translation units (e.g. -D tuning knobs of trace.cuh / render.cu)."""
+    OUT = Path(out_dir) if out_dir else globals()["OUT"]
+    LIB = OUT / "libcsgrt.so"
     OUT.mkdir(parents=True, exist_ok=True)
     cuda = cuda_home()
     inc = [f"-I{ROOT / 'include'}", f"-I{CSRC}", f"-I{cuda / 'include'}"]

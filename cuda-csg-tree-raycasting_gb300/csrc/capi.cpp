@@ -165,6 +165,7 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
     s->dev.live_words = pk.live_words;
     s->dev.live_shift = pk.live_shift;
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
+    s->dev.rolled = csgrt::use_rolled(s->tree) ? 1 : 0;
     s->status = reinterpret_cast<unsigned long long*>(base + off_status);
     *out = s;
     return CSG_OK;

@@ -68,8 +68,13 @@ inline size_t smem_bytes(int sd, int live_words)
            (size_t)(kThreads / 32) * dev::kWarpStack * 4;
 }
 
-template <int SD>
-__global__ void __launch_bounds__(kThreads) render_tiled(const RenderParams p)
+// Minimum resident blocks per SM asked of the register allocator for the rolled variant
+// (a tuning knob; the unrolled variant fits in 72 registers on its own).
+#ifndef CSG_ROLLED_MIN_BLOCKS
+#define CSG_ROLLED_MIN_BLOCKS 1
+#endif
+template <int SD, bool ROLLED>
+__global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : 1) render_tiled(const RenderParams p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint16_t tab[27];
@@ -100,29 +105,36 @@ __global__ void __launch_bounds__(kThreads) render_tiled(const RenderParams p)
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h);
     // every lane of the warp takes part in the pre-pass walk; lanes outside the image
     // only follow it
-    dev::live_prepass(ray, inside, p.scene, lm, wstacks + warp * dev::kWarpStack);
+    dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, wstacks + warp * dev::kWarpStack);
     if (!inside) return;
     bool capped = false;
-    const dev::Hit h = dev::csg_traverse<SD>(p.scene, ray, st, tab, lm, p.iter_cap, &capped);
+    const dev::Hit h = dev::csg_traverse<SD, ROLLED>(p.scene, ray, st, tab, lm, p.iter_cap, &capped);
     write_pixel(p, ray, h, capped, x, y);
 }
 
-template <int SD>
-cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
+template <int SD, bool ROLLED>
+cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
     const size_t smem = smem_bytes(SD, p.scene.live_words);
     // Above the default 48 KiB per block the kernel needs the opt-in; set it once for the
     // largest layout any scene can ask for (kLiveWordsMax live words).
     static bool attr_set = false;
     if (!attr_set) {
-        const cudaError_t e = cudaFuncSetAttribute(render_tiled<SD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        const cudaError_t e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                    (int)smem_bytes(SD, kLiveWordsMax));
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
     const dim3 grid((p.w + kTileW - 1) / kTileW, (p.h + kTileH - 1) / kTileH);
-    render_tiled<SD><<<grid, kThreads, smem, stream>>>(p);
+    render_tiled<SD, ROLLED><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
+}
+
+template <int SD>
+cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
+{
+    return p.scene.rolled ? launch_variant<SD, true>(p, stream) : launch_variant<SD, false>(p, stream);
 }
 
 __global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fdiv_rn(fov, 2.0f)); }

@@ -284,6 +284,14 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err)
 
 bool use_prepass(int32_t n_prims) { return n_prims >= 8; }
 
+bool use_rolled(const HostTree& tree)
+{
+    if (tree.prims.size() <= 8) return false;
+    for (const RefNode& n : tree.nodes)
+        if (n.type == kCylinder) return true;
+    return false;
+}
+
 int32_t stack_class_for_depth(int32_t op_depth)
 {
     if (op_depth <= 4) return 4;

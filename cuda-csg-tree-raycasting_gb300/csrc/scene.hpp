@@ -81,6 +81,7 @@ struct DeviceScene {
     int32_t live_words = 0;   // words of the per-ray live mask
     int32_t live_shift = 0;   // log2 of the leaves per live bit
     int32_t prepass = 0;      // run the liveness pre-pass (scenes with enough leaves)
+    int32_t rolled = 0;       // kernel variant: GoTo's tests in a rolled loop (see trace.cuh)
 };
 
 // Host image of the device arrays (for upload and for tests).
@@ -105,5 +106,11 @@ int32_t stack_class_for_depth(int32_t op_depth);
 // Whether renders of a scene with this many primitives run the liveness pre-pass (for a
 // handful of primitives the pre-pass costs more than the pruning saves).
 bool use_prepass(int32_t n_prims);
+
+// Kernel variant for a tree: the rolled GoTo loop when the tree has cylinders and more
+// than a handful of primitives (the code of three primitive tests unrolled twice overflows
+// the instruction cache), the unrolled one otherwise (it overlaps the two children's
+// tests).
+bool use_rolled(const HostTree& tree);
 
 }  // namespace csgrt

@@ -147,7 +147,9 @@ __device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float
 
 // isBVHNodeHit (RaycastingKernels.cu:718-756): slab test with six divisions.
 // Returns true when the box must be entered (a cull sets hit = Miss in the caller).
-__device__ __forceinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
+// Out of line: taken only by the rare rays the certified test below cannot decide, and
+// its six IEEE divisions are a lot of code to inline at every call site.
+__device__ __noinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
 {
     const float t1 = __fdiv_rn(__fsub_rn(lo.x, r.o.x), r.d.x);
     const float t2 = __fdiv_rn(__fsub_rn(hi.x, r.o.x), r.d.x);
@@ -530,6 +532,7 @@ __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* 
 // primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
 // active == false only follow.  If the walk would overflow the warp's stack, every lane
 // falls back to an all-live mask (the traversal then decides everything itself).
+template <bool ROLLED>
 __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LiveMask& lm,
                                              int* wstack)
 {
@@ -548,10 +551,23 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
         const float4 a2 = __ldg(&bvh[4 * node + 2]);
         const float4 a3 = __ldg(&bvh[4 * node + 3]);
         const int cl = __float_as_int(a0.w), cr = __float_as_int(a2.w);
-        const bool hl = active && box_hit(ray, a0, a1, 0.0f);
-        const bool hr = active && box_hit(ray, a2, a3, 0.0f);
-        if (hl && cl < 0 && leaf_live_at_zero(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
-        if (hr && cr < 0 && leaf_live_at_zero(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
+        bool hl = false, hr = false;
+        if (ROLLED) {
+#pragma unroll 1
+            for (int j = 0; j < 2; ++j) {
+                const float4 lo = j ? a2 : a0, hi = j ? a3 : a1;
+                const int c = j ? cr : cl;
+                const bool h = active && box_hit(ray, lo, hi, 0.0f);
+                if (h && c < 0 && leaf_live_at_zero(ray, sc.geo, ~c, __float_as_int(hi.w))) lm.set_leaf(~c);
+                if (j) hr = h;
+                else hl = h;
+            }
+        } else {
+            hl = active && box_hit(ray, a0, a1, 0.0f);
+            hr = active && box_hit(ray, a2, a3, 0.0f);
+            if (hl && cl < 0 && leaf_live_at_zero(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
+            if (hr && cr < 0 && leaf_live_at_zero(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
+        }
         const bool dl = __any_sync(0xffffffffu, hl && cl >= 0);
         const bool dr = __any_sync(0xffffffffu, hr && cr >= 0);
         if (dl && dr) {
@@ -589,8 +605,12 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 //  * sphere: the sphere test runs first; only a hit is confirmed with the box test;
 //  * cylinder: its box is not conservative (BVHNode.cuh:34-49) and does cut hits, so the
 //    box test runs first, as in the reference.
+//
+// With boxed == false the same code serves GoTo landing on a leaf (the root is a leaf, or a
+// loop re-enters a leaf child), where the reference calls hitPrimitive with no box test.
 __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restrict__ geo, float4 lo, float4 hi,
-                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LiveMask& lm)
+                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LiveMask& lm,
+                                           bool boxed = true)
 {
     if (!lm.any(leaf_lo, leaf_hi)) {
         H.hit = kMiss;
@@ -609,16 +629,18 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
     const float4 g0 = __ldg(&geo[2 * prim]);
     if (type == kSphere) {
         sphere_hit(ray, g0, prim, H, tmin);
-        if (H.hit != kMiss && !box_hit(ray, lo, hi, tmin)) H.hit = kMiss;
+        if (boxed && H.hit != kMiss && !box_hit(ray, lo, hi, tmin)) H.hit = kMiss;
     } else if (type == kCube) {
         cube_hit(ray, g0, prim, H, tmin);
-    } else {
-        if (box_hit(ray, lo, hi, tmin)) {
+    } else if (type == kCylinder) {
+        if (!boxed || box_hit(ray, lo, hi, tmin)) {
             const float4 g1 = __ldg(&geo[2 * prim + 1]);
             cylinder_hit(ray, g0, g1, prim, H, tmin);
         } else {
             H.hit = kMiss;
         }
+    } else {
+        H = hit_default();
     }
     if (H.hit == kMiss) lm.clear_leaf(prim);
     return false;
@@ -678,7 +700,11 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
 
 // One iteration of the CSGRayCast loop: SaveLft, GoTo (:514-595), Compute (:597-661) with
 // LookUpActions (:664-706).  `tab` is the 27-entry table in shared memory.
-template <int SD>
+// ROLLED evaluates GoTo's tests (both children of an operator, or the leaf GoTo landed on)
+// in one rolled loop, so the primitive tests exist once in the code; the unrolled form
+// overlaps the two children's tests and is faster when the code stays small (scenes
+// without cylinders).
+template <int SD, bool ROLLED>
 __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, SmemStacks<SD>& st,
                                             const uint16_t* tab, LiveMask& lm)
 {
@@ -696,15 +722,54 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
     if (T.action & (kGotoL | kGotoR)) {
         T.cur = (T.action & kGotoL) ? T.ct.x : T.ct.y;
         T.ct = __ldg(&topo[T.cur]);
-        if (T.ct.w <= kIntersection) {
+        const bool op = T.ct.w <= kIntersection;
+        bool gl = false, gr = false;
+        if (ROLLED) {
+            const float4* kn = &kids[kKidsPerNode * T.cur];
+            const int nj = op ? 2 : 1;
+            const bool leaf_right = !op && (T.action & kGotoR);
+#pragma unroll 1
+            for (int j = 0; j < nj; ++j) {
+                float4 lo, hi;
+                int rlo, rhi;
+                if (op) {
+                    lo = __ldg(&kn[2 * j]);
+                    hi = __ldg(&kn[2 * j + 1]);
+                    const int2 rg = __ldg(reinterpret_cast<const int2*>(&kn[4]) + j);
+                    rlo = rg.x;
+                    rhi = rg.y;
+                } else {
+                    // GoTo landed on a leaf: one unboxed test into L or R
+                    lo = make_float4(0.f, 0.f, 0.f, __int_as_float(T.ct.w));
+                    hi = make_float4(0.f, 0.f, 0.f, __int_as_float(T.ct.x));
+                    rlo = rhi = T.ct.x;
+                }
+                const bool right = (j == 1) || leaf_right;
+                Hit H = right ? T.R : T.L;
+                const bool go = child_test(T.ray, geo, lo, hi, rlo, rhi, H, T.tmin, lm, op);
+                if (right) {
+                    T.R = H;
+                    gr = go;
+                } else {
+                    T.L = H;
+                    gl = go;
+                }
+            }
+        } else if (op) {
             const float4* kn = &kids[kKidsPerNode * T.cur];
             const float4 k0 = __ldg(&kn[0]);
             const float4 k1 = __ldg(&kn[1]);
             const float4 k2 = __ldg(&kn[2]);
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
-            const bool gl = child_test(T.ray, geo, k0, k1, rg.x, rg.y, T.L, T.tmin, lm);
-            const bool gr = child_test(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
+            gl = child_test(T.ray, geo, k0, k1, rg.x, rg.y, T.L, T.tmin, lm);
+            gr = child_test(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
+        } else {
+            Hit& H = (T.action & kGotoL) ? T.L : T.R;
+            hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
+            if (H.hit == kMiss) lm.clear_leaf(T.ct.x);
+        }
+        if (op) {
             if (gl || gr) {
                 if (!gl) {
                     st.ppush(T.L);
@@ -724,9 +789,6 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
                 T.action = kCompute;
             }
         } else {
-            Hit& H = (T.action & kGotoL) ? T.L : T.R;
-            hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
-            if (H.hit == kMiss) lm.clear_leaf(T.ct.x);
             T.action = T.as.pop();
             tracer_parent(T, topo);
         }
@@ -777,7 +839,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
 
 // Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
 // stopped at iter_cap; *capped is then set).
-template <int SD>
+template <int SD, bool ROLLED>
 __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, SmemStacks<SD>& st,
                                             const uint16_t* tab, LiveMask& lm, uint32_t iter_cap, bool* capped)
 {
@@ -789,7 +851,7 @@ __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ra
             *capped = true;
             return hit_default();
         }
-        tracer_step<SD>(T, sc, st, tab, lm);
+        tracer_step<SD, ROLLED>(T, sc, st, tab, lm);
     }
     *capped = false;
     return T.L;
