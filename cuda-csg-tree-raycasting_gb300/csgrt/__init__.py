@@ -37,6 +37,8 @@ EXPORTED = [
     "csg_camera_move", "csg_camera_rotate", "csg_light_dir", "csg_light_default",
     "csg_render", "csg_render_f4", "csg_render_planes", "csg_scene_check", "csg_device_tan_half_fov",
     "csg_probe_fp32_peak",
+    "csg_batch_create", "csg_batch_destroy", "csg_batch_render", "csg_batch_set_tile", "csg_batch_tune",
+    "csg_batch_get_info", "csg_batch_check",
 ]
 
 _vp = ctypes.c_void_p
@@ -63,6 +65,16 @@ class csg_scene_info(ctypes.Structure):
 
 class csg_planes(ctypes.Structure):
     _fields_ = [("rgba8", _vp), ("rgba32f", _vp), ("t", _vp), ("prim", _vp), ("normal", _vp)]
+
+
+class csg_view(ctypes.Structure):
+    _fields_ = [("scene", _vp), ("cam", csg_camera), ("light_dir", _f * 3), ("w", _i32), ("h", _i32),
+                ("out", csg_planes)]
+
+
+class csg_batch_info(ctypes.Structure):
+    _fields_ = [("n_views", _i32), ("n_items", _i32), ("warp_tile_w", _i32), ("stack_class", _i32),
+                ("rolled", _i32), ("grid", _i32), ("device_bytes", ctypes.c_uint64)]
 
 
 _LIB = None
@@ -106,6 +118,13 @@ def lib() -> ctypes.CDLL:
     L.csg_scene_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_device_tan_half_fov.argtypes = [_f, ctypes.POINTER(_f)]
     L.csg_probe_fp32_peak.argtypes = [ctypes.POINTER(_f), ctypes.POINTER(_f)]
+    L.csg_batch_create.argtypes = [ctypes.POINTER(csg_view), _i32, ctypes.POINTER(_vp)]
+    L.csg_batch_destroy.argtypes = [_vp]
+    L.csg_batch_render.argtypes = [_vp, _vp]
+    L.csg_batch_set_tile.argtypes = [_vp, _i32]
+    L.csg_batch_tune.argtypes = [_vp, _vp, ctypes.POINTER(_i32), ctypes.POINTER(_f)]
+    L.csg_batch_get_info.argtypes = [_vp, ctypes.POINTER(csg_batch_info)]
+    L.csg_batch_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     _LIB = L
     return L
 
@@ -282,6 +301,65 @@ class Scene:
     def check(self, stream=0) -> int:
         n = ctypes.c_uint64()
         rc = lib().csg_scene_check(self.h, stream or None, ctypes.byref(n))
+        if rc not in (CSG_OK, CSG_E_TIMEOUT):
+            check(rc)
+        return int(n.value)
+
+
+# ------------------------------------------------------------------------------------
+class Batch:
+    """Many views of many scenes rendered by one persistent, graph-replayed launch.
+
+    `views` is a list of (scene, camera, light, w, h, planes) where planes maps plane names
+    ("rgba8", "rgba32f", "t", "prim", "normal") to device pointers.  The scenes and the
+    planes must outlive the batch."""
+
+    def __init__(self, views):
+        arr = (csg_view * len(views))()
+        for i, (scene, cam, light, w, h, planes) in enumerate(views):
+            v = arr[i]
+            v.scene = scene.h
+            ctypes.memmove(ctypes.byref(v.cam), ctypes.byref(cam.c), 60)
+            for k in range(3):
+                v.light_dir[k] = float(light[k])
+            v.w, v.h = int(w), int(h)
+            v.out = csg_planes(planes.get("rgba8") or None, planes.get("rgba32f") or None, planes.get("t") or None,
+                               planes.get("prim") or None, planes.get("normal") or None)
+        h = _vp()
+        check(lib().csg_batch_create(arr, len(views), ctypes.byref(h)))
+        self.h = h
+        self._keep = views
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().csg_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def render(self, stream=0):
+        check(lib().csg_batch_render(self.h, stream or None))
+
+    def set_tile(self, warp_tile_w: int):
+        check(lib().csg_batch_set_tile(self.h, warp_tile_w))
+
+    def tune(self, stream=0):
+        tw, ms = _i32(), _f()
+        check(lib().csg_batch_tune(self.h, stream or None, ctypes.byref(tw), ctypes.byref(ms)))
+        return tw.value, ms.value
+
+    def info(self) -> dict:
+        inf = csg_batch_info()
+        check(lib().csg_batch_get_info(self.h, ctypes.byref(inf)))
+        return {k: getattr(inf, k) for k, _ in csg_batch_info._fields_}
+
+    def check(self, stream=0) -> int:
+        n = ctypes.c_uint64()
+        rc = lib().csg_batch_check(self.h, stream or None, ctypes.byref(n))
         if rc not in (CSG_OK, CSG_E_TIMEOUT):
             check(rc)
         return int(n.value)

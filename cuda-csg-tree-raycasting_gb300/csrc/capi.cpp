@@ -11,15 +11,8 @@
 
 #include "render.hpp"
 #include "scene.hpp"
+#include "scene_handle.hpp"
 
-struct csg_scene {
-    csgrt::HostTree tree;
-    csgrt::DeviceScene dev;
-    void* dmem = nullptr;
-    size_t bytes = 0;
-    unsigned long long* status = nullptr;
-    int device = 0;
-};
 
 namespace {
 

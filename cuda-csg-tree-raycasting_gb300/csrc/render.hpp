@@ -20,6 +20,15 @@ struct Camera {
     float v[15];  // x y z rotX rotY fov forward[3] right[3] up[3] (reference Camera layout)
 };
 
+// Everything one view needs: scene, camera, light, size, output planes.
+struct ViewParams {
+    DeviceScene scene;
+    Camera cam;
+    float light[3];
+    int32_t w, h;
+    Planes out;
+};
+
 // Per-ray iteration cap of the traversal loop.  The reference has none; the largest
 // count seen on the reference scenes is a few thousand (testCheese512), so the cap is
 // never reached by a well-formed tree and only stops a runaway ray on a shared GPU.

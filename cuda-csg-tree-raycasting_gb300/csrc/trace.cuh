@@ -149,7 +149,7 @@ __device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float
 // Returns true when the box must be entered (a cull sets hit = Miss in the caller).
 // Out of line: taken only by the rare rays the certified test below cannot decide, and
 // its six IEEE divisions are a lot of code to inline at every call site.
-__device__ __noinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
+static __device__ __noinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
 {
     const float t1 = __fdiv_rn(__fsub_rn(lo.x, r.o.x), r.d.x);
     const float t2 = __fdiv_rn(__fsub_rn(hi.x, r.o.x), r.d.x);

@@ -124,6 +124,46 @@ int csg_render_planes(const csg_scene* scene, const csg_camera* cam, const float
  * call stopped at the traversal iteration cap (CSG_E_TIMEOUT if any, else CSG_OK). */
 int csg_scene_check(const csg_scene* scene, void* stream, uint64_t* n_capped);
 
+/* ---- batches: many views of many scenes in one persistent launch --------------------
+ * No counterpart in the reference, which renders one view per Raycast call; the per-view
+ * results are the same bytes csg_render_planes writes. */
+typedef struct csg_view {
+    const csg_scene* scene;
+    csg_camera cam;
+    float light_dir[3];
+    int32_t w, h;
+    csg_planes out;   /* device planes of this view (any may be NULL) */
+} csg_view;
+
+typedef struct csg_batch csg_batch;
+
+typedef struct csg_batch_info {
+    int32_t n_views;
+    int32_t n_items;      /* 128-pixel block tiles in the work list */
+    int32_t warp_tile_w;  /* warp tile width (height = 32 / width) */
+    int32_t stack_class;  /* kernel variant: stack capacity ... */
+    int32_t rolled;       /* ... and rolled GoTo loop */
+    int32_t grid;         /* persistent blocks */
+    uint64_t device_bytes;
+} csg_batch_info;
+
+/* Builds the view descriptors and the longest-first work list on the current device.
+ * The scenes and the output planes must stay valid while the batch is used. */
+int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out);
+int csg_batch_destroy(csg_batch* batch);
+/* Renders every view in one persistent launch, replayed from a CUDA graph captured on the
+ * first call (and again after a tile change); asynchronous on `stream`. */
+int csg_batch_render(csg_batch* batch, void* stream);
+/* Sets the warp tile width (4, 8, 16 or 32 pixels; height 32 / width). */
+int csg_batch_set_tile(csg_batch* batch, int32_t warp_tile_w);
+/* Autotuner: renders the batch with every warp tile shape, keeps the fastest, and reports
+ * it and its time.  Synchronous. */
+int csg_batch_tune(csg_batch* batch, void* stream, int32_t* best_tile_w, float* best_ms);
+int csg_batch_get_info(const csg_batch* batch, csg_batch_info* info);
+/* Synchronises `stream`; number of rays of the batch's renders stopped at the iteration
+ * cap since the last call (CSG_E_TIMEOUT if any). */
+int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
+
 /* ---- misc ---------------------------------------------------------------------------- */
 /* Diagnostic: tan(fov / 2) as the device's ray generation computes it (RaycastingKernels.cu
  * :15-16 evaluates tan on the device).  Synchronous.  For checkers that restate the ray
