@@ -38,7 +38,7 @@ EXPORTED = [
     "csg_render", "csg_render_f4", "csg_render_planes", "csg_scene_check", "csg_device_tan_half_fov",
     "csg_probe_fp32_peak",
     "csg_batch_create", "csg_batch_destroy", "csg_batch_render", "csg_batch_set_tile", "csg_batch_tune",
-    "csg_batch_get_info", "csg_batch_check",
+    "csg_batch_get_info", "csg_batch_check", "csg_render_views_noalloc",
 ]
 
 _vp = ctypes.c_void_p
@@ -125,6 +125,7 @@ def lib() -> ctypes.CDLL:
     L.csg_batch_tune.argtypes = [_vp, _vp, ctypes.POINTER(_i32), ctypes.POINTER(_f)]
     L.csg_batch_get_info.argtypes = [_vp, ctypes.POINTER(csg_batch_info)]
     L.csg_batch_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
+    L.csg_render_views_noalloc.argtypes = [ctypes.POINTER(csg_view), _i32, _i32, _vp]
     _LIB = L
     return L
 

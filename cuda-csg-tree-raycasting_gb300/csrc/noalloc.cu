@@ -1,0 +1,274 @@
+// csg_render_views_noalloc: the batched persistent render (batch.cu) for callers that must
+// not allocate device memory.
+//
+// Some callers cannot allocate at render time.  A server running at its device-memory
+// budget has no headroom for a per-request batch object, and a failed cudaMalloc there
+// would drop the request.  A frame loop cannot afford cudaFree, which synchronises the
+// whole device and stalls every other stream.  This entry point therefore keeps all of
+// its scratch -- the work counter, the view table and the per-view tile prefix -- in one
+// file-scope device array of fixed size (kScratchBytes, room for kMaxViews views), and
+// the call itself allocates nothing on the device or on the host heap.  The descriptors
+// are built in fixed-size stack buffers and reach the array as kernel parameters of small
+// fill launches (so no host buffer has to outlive the call, and no copy from pageable
+// memory is involved).
+//
+// Work items are not listed: item i is block tile i - prefix[v] of the view v found by a
+// binary search of the tile prefix, and the views are stored longest-first, so the launch
+// needs O(views) scratch rather than the O(tiles) work list of csg_batch.  The per-pixel
+// code is pix::render_pixel, shared with the single-view and batched kernels, so every
+// view's planes are the bytes csg_render_planes writes.
+//
+// Only the work counter must start at zero; every call's first fill launch clears it on
+// the call's stream, ahead of the render launch.  Rays stopped at the iteration cap are
+// counted in each view's scene, as csg_render_planes counts them, and csg_scene_check
+// reports them.
+//
+// All calls share the one array per device: two calls whose work can overlap on the
+// device (different streams, or different host threads without ordering) race on it and
+// must be serialised by the caller.
+#include <algorithm>
+#include <atomic>
+#include <climits>
+#include <cstring>
+
+#include "csgrt.h"
+#include "pixel.cuh"
+#include "scene_handle.hpp"
+
+namespace csgrt {
+namespace {
+
+using pix::kThreads;
+
+constexpr int kMaxViews = CSG_NOALLOC_MAX_VIEWS;
+
+struct NoAllocView {
+    ViewParams view;
+    unsigned long long* status;  // the scene's capped-ray counter
+    int32_t tiles_x;              // block tiles per row
+    int32_t pad;
+};
+
+// Scratch layout: [work counter | pad to 256 B][views, longest first][tile prefix].
+constexpr size_t kViewsOffset = 256;
+constexpr size_t kPrefixOffset = kViewsOffset + sizeof(NoAllocView) * kMaxViews;
+constexpr size_t kScratchBytes = 1u << 20;
+static_assert(kPrefixOffset + sizeof(int32_t) * (kMaxViews + 1) <= kScratchBytes, "scratch too small");
+static_assert(sizeof(NoAllocView) % 8 == 0, "view record alignment");
+
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+struct NoAllocLaunch {
+    const NoAllocView* views;
+    const int32_t* prefix;  // prefix[v] = first item of view v; prefix[n_views] = n_items
+    int* counter;
+    int32_t n_views;
+    int32_t n_items;
+    int32_t tw_log2;
+    int32_t live_words;
+    uint32_t iter_cap;
+};
+
+template <int SD, bool ROLLED>
+__global__ void __launch_bounds__(kThreads) render_views_noalloc(const NoAllocLaunch p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint16_t tab[27];
+    __shared__ int s_item, s_view;
+    pix::load_table(tab);
+    dev::SmemStacks<SD> st = pix::block_stacks<SD>(smem_raw);
+    const pix::BlockSmem bs = pix::block_smem<SD>(smem_raw, p.live_words);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tw = 1 << p.tw_log2, th = 32 >> p.tw_log2;
+    const int ox = (warp & 1) * tw + (lane & (tw - 1));
+    const int oy = (warp >> 1) * th + (lane >> p.tw_log2);
+    while (true) {
+        __syncthreads();  // everyone has read s_item / s_view before they are overwritten
+        if (threadIdx.x == 0) {
+            const int it = atomicAdd(p.counter, 1);
+            int lo = 0, hi = p.n_views - 1;  // last view whose first item is <= it
+            if (it < p.n_items) {
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (p.prefix[mid] <= it) lo = mid;
+                    else hi = mid - 1;
+                }
+            }
+            s_item = it;
+            s_view = lo;
+        }
+        __syncthreads();
+        const int it = s_item;
+        if (it >= p.n_items) break;
+        const NoAllocView& v = p.views[s_view];
+        const int tile = it - p.prefix[s_view];
+        const int tx = tile % v.tiles_x, ty = tile / v.tiles_x;
+        const int x = tx * 2 * tw + ox, y = ty * 2 * th + oy;
+        const bool inside = x < v.view.w && y < v.view.h;
+        pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab);
+    }
+}
+
+// One fill launch: up to kChunk view records and their tile prefixes, passed by value.
+constexpr int kChunk = 112;
+struct FillChunk {
+    NoAllocView rec[kChunk];
+    int32_t prefix[kChunk];
+    int32_t k0, n;       // first view slot, records in this chunk
+    int32_t total;       // items of the whole call (written after the last view's prefix)
+    int32_t last;        // this chunk holds the last view
+};
+static_assert(sizeof(FillChunk) <= 32000, "kernel parameter space");
+
+__global__ void fill_scratch(const __grid_constant__ FillChunk c, unsigned char* scratch)
+{
+    constexpr int kWords = sizeof(NoAllocView) / 8;
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(&c.rec[0]);
+    uint64_t* dst = reinterpret_cast<uint64_t*>(scratch + kViewsOffset + sizeof(NoAllocView) * c.k0);
+    for (int i = threadIdx.x; i < c.n * kWords; i += blockDim.x) dst[i] = src[i];
+    int32_t* pf = reinterpret_cast<int32_t*>(scratch + kPrefixOffset);
+    for (int i = threadIdx.x; i < c.n; i += blockDim.x) pf[c.k0 + i] = c.prefix[i];
+    if (threadIdx.x == 0) {
+        if (c.last) pf[c.k0 + c.n] = c.total;
+        if (c.k0 == 0) *reinterpret_cast<int*>(scratch) = 0;  // the work counter
+    }
+}
+
+template <int SD, bool ROLLED>
+cudaError_t launch_variant(const NoAllocLaunch& l, int device, cudaStream_t stream)
+{
+    const auto kernel = render_views_noalloc<SD, ROLLED>;
+    const size_t smem = pix::smem_bytes(SD, l.live_words);
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int sms = 0, per_sm = 0;
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
+    if (e != cudaSuccess) return e;
+    int grid = sms * std::max(per_sm, 1);
+    grid = std::max(1, std::min(grid, l.n_items));
+    kernel<<<grid, kThreads, smem, stream>>>(l);
+    return cudaGetLastError();
+}
+
+cudaError_t dispatch(const NoAllocLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
+{
+    switch (stack_class) {
+        case 4: return rolled ? launch_variant<4, true>(l, device, stream) : launch_variant<4, false>(l, device, stream);
+        case 8: return rolled ? launch_variant<8, true>(l, device, stream) : launch_variant<8, false>(l, device, stream);
+        case 12:
+            return rolled ? launch_variant<12, true>(l, device, stream) : launch_variant<12, false>(l, device, stream);
+        case 16:
+            return rolled ? launch_variant<16, true>(l, device, stream) : launch_variant<16, false>(l, device, stream);
+        default:
+            return rolled ? launch_variant<32, true>(l, device, stream) : launch_variant<32, false>(l, device, stream);
+    }
+}
+
+// Address of the scratch array on each device, looked up on the first call there.
+constexpr int kMaxDevices = 64;
+std::atomic<unsigned char*> g_scratch_addr[kMaxDevices];
+
+unsigned char* scratch_on(int device)
+{
+    if (device < 0 || device >= kMaxDevices) return nullptr;
+    unsigned char* p = g_scratch_addr[device].load(std::memory_order_acquire);
+    if (p) return p;
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_scratch) != cudaSuccess || !addr) return nullptr;
+    p = static_cast<unsigned char*>(addr);
+    g_scratch_addr[device].store(p, std::memory_order_release);
+    return p;
+}
+
+double view_cost(const csg_view& v)
+{
+    return (double)v.w * (double)v.h * (1.0 + v.scene->dev.n_prims);
+}
+
+}  // namespace
+}  // namespace csgrt
+
+extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream)
+{
+    using namespace csgrt;
+    if (!views || n_views <= 0) return CSG_E_ARG;
+    if (n_views > kMaxViews) return CSG_E_CAPACITY;
+    if (warp_tile_w == 0) warp_tile_w = 8;
+    if (warp_tile_w != 4 && warp_tile_w != 8 && warp_tile_w != 16 && warp_tile_w != 32) return CSG_E_ARG;
+    const int tw = warp_tile_w, th = 32 / warp_tile_w;
+    int32_t sd = 4, live = 1;
+    bool rolled = false;
+    for (int32_t i = 0; i < n_views; ++i) {
+        const csg_view& v = views[i];
+        if (!v.scene || v.w <= 0 || v.h <= 0) return CSG_E_ARG;
+        if (v.out.rgba32f && (reinterpret_cast<uintptr_t>(v.out.rgba32f) & 15u)) return CSG_E_ARG;
+        sd = std::max(sd, v.scene->dev.stack_class);
+        live = std::max(live, v.scene->dev.live_words);
+        rolled = rolled || v.scene->dev.rolled;
+    }
+    int device = 0;
+    if (cudaGetDevice(&device) != cudaSuccess) return CSG_E_CUDA;
+    unsigned char* scratch = scratch_on(device);
+    if (!scratch) return CSG_E_CUDA;
+
+    // Longest-first order and the tile prefix, in fixed-size stack buffers.
+    int32_t order[kMaxViews];
+    int32_t prefix[kMaxViews + 1];
+    for (int32_t i = 0; i < n_views; ++i) order[i] = i;
+    std::sort(order, order + n_views, [&](int32_t a, int32_t b) {
+        const double ca = view_cost(views[a]), cb = view_cost(views[b]);
+        return ca > cb || (ca == cb && a < b);
+    });
+    long long total = 0;
+    for (int32_t k = 0; k < n_views; ++k) {
+        const csg_view& v = views[order[k]];
+        prefix[k] = static_cast<int32_t>(total);
+        total += (long long)((v.w + 2 * tw - 1) / (2 * tw)) * ((v.h + 2 * th - 1) / (2 * th));
+        if (total > INT_MAX) return CSG_E_CAPACITY;
+    }
+    prefix[n_views] = static_cast<int32_t>(total);
+
+    // View records and prefixes, by value through the fill launches' parameters.
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    FillChunk c;
+    for (int32_t k0 = 0; k0 < n_views; k0 += kChunk) {
+        const int32_t n = std::min<int32_t>(kChunk, n_views - k0);
+        for (int32_t j = 0; j < n; ++j) {
+            const csg_view& v = views[order[k0 + j]];
+            NoAllocView& r = c.rec[j];
+            r = NoAllocView{};
+            r.view.scene = v.scene->dev;
+            std::memcpy(r.view.cam.v, &v.cam, sizeof(r.view.cam.v));
+            r.view.light[0] = v.light_dir[0];
+            r.view.light[1] = v.light_dir[1];
+            r.view.light[2] = v.light_dir[2];
+            r.view.w = v.w;
+            r.view.h = v.h;
+            r.view.out.rgba8 = v.out.rgba8;
+            r.view.out.rgba32f = reinterpret_cast<float4*>(v.out.rgba32f);
+            r.view.out.t = v.out.t;
+            r.view.out.prim = v.out.prim;
+            r.view.out.normal = v.out.normal;
+            r.status = v.scene->status;
+            r.tiles_x = (v.w + 2 * tw - 1) / (2 * tw);
+            c.prefix[j] = prefix[k0 + j];
+        }
+        c.k0 = k0;
+        c.n = n;
+        c.total = static_cast<int32_t>(total);
+        c.last = (k0 + n == n_views) ? 1 : 0;
+        fill_scratch<<<1, 256, 0, st>>>(c, scratch);
+        if (cudaGetLastError() != cudaSuccess) return CSG_E_CUDA;
+    }
+
+    NoAllocLaunch l;
+    l.views = reinterpret_cast<const NoAllocView*>(scratch + kViewsOffset);
+    l.prefix = reinterpret_cast<const int32_t*>(scratch + kPrefixOffset);
+    l.counter = reinterpret_cast<int*>(scratch);
+    l.n_views = n_views;
+    l.n_items = static_cast<int32_t>(total);
+    l.tw_log2 = tw == 4 ? 2 : tw == 8 ? 3 : tw == 16 ? 4 : 5;
+    l.live_words = live;
+    l.iter_cap = kIterCap;
+    return dispatch(l, stack_class_for_depth(sd), rolled, device, st) == cudaSuccess ? CSG_OK : CSG_E_CUDA;
+}

@@ -164,6 +164,21 @@ int csg_batch_get_info(const csg_batch* batch, csg_batch_info* info);
  * cap since the last call (CSG_E_TIMEOUT if any). */
 int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
 
+/* ---- batched render without allocation ----------------------------------------------
+ * No counterpart in the reference.  Renders up to CSG_NOALLOC_MAX_VIEWS views in one
+ * persistent launch, like csg_batch_render, but allocates no memory: its scratch (work
+ * counter, view table, tile prefix; 1 MiB) is a fixed array in the library's device
+ * image.  For callers that cannot allocate at render time -- a server at its
+ * device-memory budget, a frame loop that cannot take the device-wide synchronisation of
+ * cudaFree.  warp_tile_w is 4, 8, 16 or 32 (0: 8).  More than CSG_NOALLOC_MAX_VIEWS views
+ * gives CSG_E_CAPACITY, before anything is enqueued.  Asynchronous on `stream`; capped
+ * rays are counted per scene (csg_scene_check).  The first call on a device does set-up
+ * (looks up the array's address, sets kernel attributes): make it before any stream
+ * capture on that device.  All calls on a device share the one array, so calls whose
+ * work may overlap (different streams, unsynchronised threads) race: serialise them. */
+#define CSG_NOALLOC_MAX_VIEWS 4096
+int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream);
+
 /* ---- misc ---------------------------------------------------------------------------- */
 /* Diagnostic: tan(fov / 2) as the device's ray generation computes it (RaycastingKernels.cu
  * :15-16 evaluates tan on the device).  Synchronous.  For checkers that restate the ray
