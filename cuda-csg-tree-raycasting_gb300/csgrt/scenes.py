@@ -181,3 +181,14 @@ def config_scene_text(config: int, seed: int = 0) -> str:
     if config == 3:
         return write_text(random_tree(seed, 2, 4096, 12))
     return write_text(random_tree(seed, 2, 2048, 12))
+
+
+def config_batch(seed: int = 0, n_scenes: int = 256, per_scene: int = 4):
+    """The batched workload: n_scenes random trees (leaf counts log-uniform 2..2048, depth
+    <= 12), each seen by per_scene seeded cameras at resolutions uniform over 256^2,
+    512^2, 768^2 and 1024^2.  Returns [(scene text, [View, ...]), ...]."""
+    out = []
+    for s in range(n_scenes):
+        sid = seed * 100003 + s
+        out.append((write_text(random_tree(sid, 2, 2048, 12)), config_views(4, sid, per_scene)))
+    return out
