@@ -45,6 +45,9 @@ WORKLOADS = {
     3: "random CSG tree (seed 0: log-uniform 2..4096 leaves, depth <= 12), 1920x1080, seeded look-at camera",
     4: "batched: 256 random trees (log-uniform 2..2048 leaves, depth <= 12) x 4 seeded cameras, per-view "
        "resolution uniform over {256,512,768,1024}^2, one persistent graph-replayed launch vs 1024 per-view launches",
+    5: "serving: Poisson arrivals at 100..5000 req/s, scenes from a pool of 1024 random trees (log-uniform "
+       "2..2048 leaves) resident under a 40 GiB budget, resolutions uniform over {256,512,1024,2048}^2, seeded "
+       "cameras; continuous batching vs one launch per request",
 }
 
 
@@ -394,6 +397,24 @@ def run_batch(args):
     pv_steps = max(2, min(args.steps, 5))
     pv_ms = timed(per_view, pv_steps)
 
+    # the reference's own kernels, one RaycastKernel + LightningKernel launch pair per view
+    ref_pv = None
+    if not args.no_reference_cuda:
+        from oracle import RefCuda
+        if RefCuda.available():
+            G = RefCuda()
+            ref_ms = 0.0
+            for text, vs in work:
+                nodes44, prims48, _ = csgrt.parse_tree(text)
+                for v in vs:
+                    o = G.render(nodes44, prims48, v.camera, v.light, v.w, v.h, reps=1, want_hits=False,
+                                 want_rgba=False)
+                    ref_ms += o["ms_frame"]
+            ref_pv = {"value": round(rays / (ref_ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+                      "ms_per_step": round(ref_ms, 2), "launches": 2 * len(views),
+                      "note": "sum over the 1024 views of the reference kernels' event-timed frame time "
+                              "(8x4 blocks, as Raycaster::Raycast launches them)"}
+
     # end to end: batched render + copy of all 1024 RGBA8 frames to pinned host memory
     flat = torch.empty(rays, dtype=torch.int32, pin_memory=True)
     offs = np.cumsum([0] + [v[3] * v[4] for v in views])
@@ -429,6 +450,8 @@ def run_batch(args):
                               "ms_per_step": round(float(np.mean(pv_ms)), 3),
                               "note": "the same 1024 views, one csg_render_planes launch each, one stream"},
         "batched_vs_per_view": round(value / ws / pv_value, 3),
+        "reference_cuda_per_view": ref_pv,
+        "batched_vs_reference_per_view": round(value / ws / ref_pv["value"], 3) if ref_pv else None,
         "gpu_launches": args.steps,
         "e2e": {"value": round(rays * e2e_steps / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": rays * 4,
@@ -442,6 +465,113 @@ def run_batch(args):
         sc.close()
     if dist:
         dist.destroy_process_group()
+
+
+def _percentile(v, q):
+    return float(np.percentile(np.asarray(v), q)) if len(v) else None
+
+
+def run_serving(args):
+    """Configuration 5: the render server under open-loop Poisson arrivals, with continuous
+    batching and with one single-view launch per request (the same server, requests
+    flagged CSG_REQ_ALONE), at swept arrival rates.  Latency = completion - scheduled
+    arrival, measured inside the library on a steady clock."""
+    import torch
+    import csgrt
+    from csgrt import scenes as S
+
+    ws, rank, local = dist_info()
+    torch.cuda.set_device(local)
+    n_pool = 1024
+    srv = csgrt.Server(hbm_budget=40 << 30, slots=4, max_batch_views=256)
+    t_setup = time.perf_counter()
+    for i in range(n_pool):
+        srv.add_scene(S.write_text(S.random_tree(500_000 + i, 2, 2048, 12)))
+    for i in range(n_pool):
+        srv.preload(i)
+    setup_s = time.perf_counter() - t_setup
+    rng = np.random.default_rng(5)
+    n_req = 256
+    sizes = [256, 512, 1024, 2048]
+
+    def make_requests(n, alone, with_host=False):
+        r2 = np.random.default_rng(rng.integers(1 << 31))
+        spec = []
+        for _ in range(n):
+            sid = int(r2.integers(0, n_pool))
+            res = sizes[int(r2.integers(0, 4))]
+            spec.append((sid, res, csgrt.Camera.look_at_origin(S.seeded_direction(r2), 4.0, 60.0)))
+        rays = sum(res * res for _, res, _ in spec)
+        host = torch.empty(rays, dtype=torch.int32, pin_memory=True) if with_host else None
+        out, offs = [], 0
+        for sid, res, cam in spec:
+            hp = host.data_ptr() + offs * 4 if with_host else 0
+            offs += res * res
+            out.append(csgrt.Server.request(sid, cam, csgrt.light_dir(), res, res, alone=alone, host_rgba8=hp))
+        return out, rays, host
+
+    # warm-up: both forms, every kernel variant the pool needs
+    for _ in range(args.warmup):
+        for alone in (False, True):
+            reqs, _, _ = make_requests(24, alone)
+            srv.replay(reqs, np.zeros(len(reqs)))
+    rates = [100, 500, 1000, 2000, 5000]
+    sweep = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        for rate in rates:
+            row = {"rate_rps": rate, "requests": n_req}
+            arrivals = np.cumsum(np.random.default_rng(rate).exponential(1.0 / rate, n_req))
+            arrivals -= arrivals[0]
+            for alone in (False, True):
+                reqs, rays, _ = make_requests(n_req, alone)
+                b0 = srv.stats()["batches"]
+                res, _, wall = srv.replay(reqs, arrivals)
+                launches += srv.stats()["batches"] - b0
+                lat = [1000.0 * (r.t_done - r.t_arrive) for r in res]
+                bad = sum(1 for r in res if r.status != 0)
+                if bad:
+                    raise RuntimeError(f"{bad} requests failed at {rate} req/s")
+                row["per_request" if alone else "batched"] = {
+                    "p50_ms": round(_percentile(lat, 50), 3), "p99_ms": round(_percentile(lat, 99), 3),
+                    "mrays_s": round(rays / wall / 1e6, 2), "wall_s": round(wall, 3),
+                    "mean_batch_views": round(float(np.mean([r.batch_views for r in res])), 2)}
+            sweep.append(row)
+        # end to end: the top rate with every RGBA8 frame copied to pinned host memory
+        top = rates[-1]
+        arrivals = np.cumsum(np.random.default_rng(top).exponential(1.0 / top, n_req))
+        arrivals -= arrivals[0]
+        reqs, rays_e2e, host = make_requests(n_req, False, with_host=True)
+        res, _, wall_e2e = srv.replay(reqs, arrivals)
+        lat_e2e = [1000.0 * (r.t_done - r.t_arrive) for r in res]
+    top_row = sweep[-1]
+    st = srv.stats()
+    srv.close()
+    if rank != 0:
+        return
+    value = top_row["batched"]["mrays_s"]
+    res_line = {
+        "metric": METRIC, "value": value, "unit": "Mrays/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(1000 * top_row["batched"]["wall_s"], 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded scene generator, seeded Poisson arrivals)",
+        "config": {"workload": WORKLOADS[5], "config_index": 5, "pool_scenes": n_pool,
+                   "requests_per_rate": n_req, "slots": 4, "max_batch_views": 256,
+                   "hbm_budget_bytes": 40 << 30, "setup_s": round(setup_s, 1),
+                   "l2": "inputs (1024 resident scenes, ~0.5 GB) and outputs exceed L2 across a run",
+                   "parallelism": "single GPU"},
+        "serving": sweep,
+        "batched_vs_per_request_at_top_rate": round(value / top_row["per_request"]["mrays_s"], 3),
+        "gpu_launches": int(launches),
+        "e2e": {"value": round(rays_e2e / wall_e2e / 1e6, 2), "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": int(rays_e2e * 4 / n_req),
+                "p50_ms": round(_percentile(lat_e2e, 50), 3), "p99_ms": round(_percentile(lat_e2e, 99), 3),
+                "note": f"{top} req/s through csg_server_submit (replay), each request's RGBA8 frame copied to "
+                        "pinned host memory before it counts as done; per-step bytes are per request"},
+        "server_stats": {k: st[k] for k in ("peak_bytes", "batches", "evictions", "rejected", "resident_scenes")},
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(res_line), flush=True)
 
 
 def run_reference(args):
@@ -481,7 +611,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4])
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
@@ -493,6 +623,8 @@ def main():
         run_reference(args)
     elif args.config == 4:
         run_batch(args)
+    elif args.config == 5:
+        run_serving(args)
     else:
         run_engine(args)
 

@@ -35,9 +35,13 @@ def _sources(names):
     return [CSRC / n for n in names if (CSRC / n).exists()]
 
 
-def build(verbose: bool = False, extra_nvcc: list[str] | None = None, out_dir: Path | None = None) -> str:
+def build(verbose: bool = False, extra_nvcc: list[str] | None = None, out_dir: Path | None = None,
+          defines: list[str] | None = None) -> str:
     """Builds libcsgrt.so into `out_dir` (default _build/); `extra_nvcc` adds flags to the
-    CUDA translation units (e.g. -D tuning knobs of trace.cuh / render.cu)."""
+    CUDA translation units (e.g. -D tuning knobs of trace.cuh / render.cu), `defines`
+    (NAME=VALUE) to every translation unit (knobs shared by host and device code, such as
+    CSG_LIVE_WORDS_MAX)."""
+    dflags = [f"-D{d}" for d in (defines or [])]
     OUT = Path(out_dir) if out_dir else globals()["OUT"]
     LIB = OUT / "libcsgrt.so"
     OUT.mkdir(parents=True, exist_ok=True)
@@ -48,14 +52,14 @@ def build(verbose: bool = False, extra_nvcc: list[str] | None = None, out_dir: P
     for src in _sources(CU_SOURCES):
         obj = OUT / (src.stem + ".cu.o")
         cmd = ["nvcc", *ARCH, "-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",
-               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *inc, *(extra_nvcc or []),
+               "-Xcompiler", "-ffp-contract=off", "-Xptxas", "-v", *inc, *dflags, *(extra_nvcc or []),
                "-c", str(src), "-o", str(obj)]
         jobs.append((src.name, cmd))
         objs.append(obj)
     for src in _sources(CPP_SOURCES):
         obj = OUT / (src.stem + ".o")
         cmd = ["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
-               "-Wno-unused-parameter", *inc, "-c", str(src), "-o", str(obj)]
+               "-Wno-unused-parameter", *inc, *dflags, "-c", str(src), "-o", str(obj)]
         jobs.append((src.name, cmd))
         objs.append(obj)
     procs = [(name, cmd, subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True))

@@ -39,6 +39,8 @@ EXPORTED = [
     "csg_probe_fp32_peak",
     "csg_batch_create", "csg_batch_destroy", "csg_batch_render", "csg_batch_set_tile", "csg_batch_tune",
     "csg_batch_get_info", "csg_batch_check", "csg_render_views_noalloc",
+    "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
+    "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
 ]
 
 _vp = ctypes.c_void_p
@@ -75,6 +77,32 @@ class csg_view(ctypes.Structure):
 class csg_batch_info(ctypes.Structure):
     _fields_ = [("n_views", _i32), ("n_items", _i32), ("warp_tile_w", _i32), ("stack_class", _i32),
                 ("rolled", _i32), ("grid", _i32), ("device_bytes", ctypes.c_uint64)]
+
+
+CSG_PLANE_RGBA8, CSG_PLANE_T, CSG_PLANE_PRIM, CSG_PLANE_NORMAL, CSG_PLANE_RGBA32F = 1, 2, 4, 8, 16
+CSG_REQ_ALONE = 1
+
+
+class csg_server_config(ctypes.Structure):
+    _fields_ = [("hbm_budget", ctypes.c_uint64), ("slots", _i32), ("max_batch_views", _i32), ("warp_tile_w", _i32),
+                ("planes", _i32), ("keep_results", _i32), ("order", _i32)]
+
+
+class csg_request(ctypes.Structure):
+    _fields_ = [("scene", _i32), ("flags", _i32), ("cam", csg_camera), ("light_dir", _f * 3), ("w", _i32),
+                ("h", _i32), ("host_rgba8", _vp)]
+
+
+class csg_result(ctypes.Structure):
+    _fields_ = [("status", _i32), ("batch_views", _i32), ("t_arrive", ctypes.c_double),
+                ("t_launch", ctypes.c_double), ("t_done", ctypes.c_double), ("planes", csg_planes)]
+
+
+class csg_server_stats(ctypes.Structure):
+    _fields_ = [("budget", ctypes.c_uint64), ("scene_bytes", ctypes.c_uint64), ("output_bytes", ctypes.c_uint64),
+                ("peak_bytes", ctypes.c_uint64), ("requests_done", ctypes.c_int64), ("batches", ctypes.c_int64),
+                ("evictions", ctypes.c_int64), ("rejected", ctypes.c_int64), ("scenes", _i32),
+                ("resident_scenes", _i32), ("slots_busy", _i32), ("pending", _i32)]
 
 
 _LIB = None
@@ -126,6 +154,20 @@ def lib() -> ctypes.CDLL:
     L.csg_batch_get_info.argtypes = [_vp, ctypes.POINTER(csg_batch_info)]
     L.csg_batch_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_render_views_noalloc.argtypes = [ctypes.POINTER(csg_view), _i32, _i32, _vp]
+    L.csg_server_create.argtypes = [ctypes.POINTER(csg_server_config), ctypes.POINTER(_vp)]
+    L.csg_server_destroy.argtypes = [_vp]
+    L.csg_server_add_scene.argtypes = [_vp, ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_i32), ctypes.c_char_p,
+                                       ctypes.c_size_t]
+    L.csg_server_preload.argtypes = [_vp, _i32]
+    L.csg_server_submit.argtypes = [_vp, ctypes.POINTER(csg_request), ctypes.POINTER(ctypes.c_int64)]
+    L.csg_server_wait.argtypes = [_vp, ctypes.c_int64, ctypes.c_double, ctypes.POINTER(csg_result)]
+    L.csg_server_release.argtypes = [_vp, ctypes.c_int64]
+    L.csg_server_replay.argtypes = [_vp, ctypes.POINTER(csg_request), ctypes.POINTER(ctypes.c_double), _i32,
+                                    ctypes.POINTER(csg_result), ctypes.POINTER(ctypes.c_int64),
+                                    ctypes.POINTER(ctypes.c_double)]
+    L.csg_server_stats_get.argtypes = [_vp, ctypes.POINTER(csg_server_stats)]
+    L.csg_server_clock.argtypes = [_vp]
+    L.csg_server_clock.restype = ctypes.c_double
     _LIB = L
     return L
 
@@ -364,3 +406,92 @@ class Batch:
         if rc not in (CSG_OK, CSG_E_TIMEOUT):
             check(rc)
         return int(n.value)
+
+
+# ------------------------------------------------------------------------------------
+class Server:
+    """Render server with continuous batching (csg_server_* of the C ABI).
+
+    Scenes are added once (parsed now, resident on first use, evicted least recently used
+    under `hbm_budget`); requests are submitted with `submit` (returns a ticket) and
+    collected with `wait`; `replay` runs an open-loop arrival trace inside the library."""
+
+    def __init__(self, hbm_budget=0, slots=0, max_batch_views=0, warp_tile_w=0, planes=0, keep_results=False,
+                 longest_first=False):
+        cfg = csg_server_config(int(hbm_budget), int(slots), int(max_batch_views), int(warp_tile_w), int(planes),
+                                1 if keep_results else 0, 1 if longest_first else 0)
+        h = _vp()
+        check(lib().csg_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().csg_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def add_scene(self, text) -> int:
+        data = text.encode() if isinstance(text, str) else bytes(text)
+        sid = _i32()
+        err = ctypes.create_string_buffer(512)
+        rc = lib().csg_server_add_scene(self.h, data, len(data), ctypes.byref(sid), err, len(err))
+        check(rc, err.value.decode(errors="replace") if rc != CSG_OK else "")
+        return sid.value
+
+    def preload(self, sid: int):
+        check(lib().csg_server_preload(self.h, sid))
+
+    @staticmethod
+    def request(scene: int, cam: "Camera", light, w: int, h: int, alone=False, host_rgba8=0) -> csg_request:
+        r = csg_request()
+        r.scene = scene
+        r.flags = CSG_REQ_ALONE if alone else 0
+        ctypes.memmove(ctypes.byref(r.cam), ctypes.byref(cam.c), 60)
+        for k in range(3):
+            r.light_dir[k] = float(light[k])
+        r.w, r.h = int(w), int(h)
+        r.host_rgba8 = host_rgba8 or None
+        return r
+
+    def submit(self, req: csg_request) -> int:
+        t = ctypes.c_int64()
+        check(lib().csg_server_submit(self.h, ctypes.byref(req), ctypes.byref(t)))
+        return t.value
+
+    def wait(self, ticket: int, timeout_s: float = -1.0) -> csg_result:
+        r = csg_result()
+        check(lib().csg_server_wait(self.h, ticket, timeout_s, ctypes.byref(r)))
+        return r
+
+    def release(self, ticket: int):
+        check(lib().csg_server_release(self.h, ticket))
+
+    def replay(self, reqs, arrival_s, keep=False):
+        """Returns (results array, tickets or None, wall seconds)."""
+        n = len(reqs)
+        arr = (csg_request * n)(*reqs)
+        at = (ctypes.c_double * n)(*[float(a) for a in arrival_s])
+        res = (csg_result * n)()
+        tk = (ctypes.c_int64 * n)() if keep else None
+        wall = ctypes.c_double()
+        check(lib().csg_server_replay(self.h, arr, at, n, res, tk, ctypes.byref(wall)))
+        return res, (list(tk) if keep else None), wall.value
+
+    def stats(self) -> dict:
+        st = csg_server_stats()
+        check(lib().csg_server_stats_get(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in csg_server_stats._fields_}
+
+    def clock(self) -> float:
+        return lib().csg_server_clock(self.h)

@@ -96,6 +96,23 @@ const char* csg_status_string(int status)
     }
 }
 
+}  // extern "C"
+
+csgrt::SceneLayout csgrt::scene_layout(size_t n_nodes, size_t n_prims, size_t n_kids_f4, size_t n_bvh_f4)
+{
+    SceneLayout l;
+    l.topo = 0;
+    l.kids = align16(l.topo + n_nodes * sizeof(int4));
+    l.geo = align16(l.kids + n_kids_f4 * sizeof(float4));
+    l.color = align16(l.geo + 2 * n_prims * sizeof(float4));
+    l.bvh = align16(l.color + n_prims * sizeof(float4));
+    l.status = align16(l.bvh + n_bvh_f4 * sizeof(float4));
+    l.total = align16(l.status + sizeof(unsigned long long));
+    return l;
+}
+
+extern "C" {
+
 int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, size_t errlen)
 {
     if (!out) return CSG_E_ARG;
@@ -113,13 +130,9 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
     csgrt::PackedScene pk;
     csgrt::pack_scene(s->tree, pk);
     const size_t n = s->tree.nodes.size(), np = s->tree.prims.size();
-    const size_t off_topo = 0;
-    const size_t off_kids = align16(off_topo + n * sizeof(int4));
-    const size_t off_geo = align16(off_kids + pk.kids.size() * sizeof(float4));
-    const size_t off_color = align16(off_geo + 2 * np * sizeof(float4));
-    const size_t off_bvh = align16(off_color + np * sizeof(float4));
-    const size_t off_status = align16(off_bvh + pk.bvh.size() * sizeof(float4));
-    const size_t total = align16(off_status + sizeof(unsigned long long));
+    const csgrt::SceneLayout lay = csgrt::scene_layout(n, np, pk.kids.size(), pk.bvh.size());
+    const size_t off_topo = lay.topo, off_kids = lay.kids, off_geo = lay.geo, off_color = lay.color;
+    const size_t off_bvh = lay.bvh, off_status = lay.status, total = lay.total;
     cudaGetDevice(&s->device);
     cudaError_t e = cudaMalloc(&s->dmem, total);
     if (e != cudaSuccess) {

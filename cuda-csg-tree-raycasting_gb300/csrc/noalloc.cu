@@ -1,5 +1,5 @@
-// csg_render_views_noalloc: the batched persistent render (batch.cu) for callers that must
-// not allocate device memory.
+// The view-table kernel (views.hpp) and csg_render_views_noalloc, the batched persistent
+// render for callers that must not allocate device memory.
 //
 // Some callers cannot allocate at render time.  A server running at its device-memory
 // budget has no headroom for a per-request batch object, and a failed cudaMalloc there
@@ -34,6 +34,7 @@
 #include "csgrt.h"
 #include "pixel.cuh"
 #include "scene_handle.hpp"
+#include "views.hpp"
 
 namespace csgrt {
 namespace {
@@ -42,35 +43,16 @@ using pix::kThreads;
 
 constexpr int kMaxViews = CSG_NOALLOC_MAX_VIEWS;
 
-struct NoAllocView {
-    ViewParams view;
-    unsigned long long* status;  // the scene's capped-ray counter
-    int32_t tiles_x;              // block tiles per row
-    int32_t pad;
-};
-
 // Scratch layout: [work counter | pad to 256 B][views, longest first][tile prefix].
 constexpr size_t kViewsOffset = 256;
-constexpr size_t kPrefixOffset = kViewsOffset + sizeof(NoAllocView) * kMaxViews;
+constexpr size_t kPrefixOffset = kViewsOffset + sizeof(ViewRecord) * kMaxViews;
 constexpr size_t kScratchBytes = 1u << 20;
 static_assert(kPrefixOffset + sizeof(int32_t) * (kMaxViews + 1) <= kScratchBytes, "scratch too small");
-static_assert(sizeof(NoAllocView) % 8 == 0, "view record alignment");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-struct NoAllocLaunch {
-    const NoAllocView* views;
-    const int32_t* prefix;  // prefix[v] = first item of view v; prefix[n_views] = n_items
-    int* counter;
-    int32_t n_views;
-    int32_t n_items;
-    int32_t tw_log2;
-    int32_t live_words;
-    uint32_t iter_cap;
-};
-
 template <int SD, bool ROLLED>
-__global__ void __launch_bounds__(kThreads) render_views_noalloc(const NoAllocLaunch p)
+__global__ void __launch_bounds__(kThreads) render_views(const ViewsLaunch p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint16_t tab[27];
@@ -100,19 +82,29 @@ __global__ void __launch_bounds__(kThreads) render_views_noalloc(const NoAllocLa
         __syncthreads();
         const int it = s_item;
         if (it >= p.n_items) break;
-        const NoAllocView& v = p.views[s_view];
-        const int tile = it - p.prefix[s_view];
+        const int vi = s_view;
+        const ViewRecord& v = p.views[vi];
+        const int tile = it - p.prefix[vi];
         const int tx = tile % v.tiles_x, ty = tile / v.tiles_x;
         const int x = tx * 2 * tw + ox, y = ty * 2 * th + oy;
         const bool inside = x < v.view.w && y < v.view.h;
         pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab);
+        if (p.remaining) {
+            if (v.host_out) __threadfence_system();  // this thread's host-mapped plane
+            else __threadfence();
+            __syncthreads();
+            if (threadIdx.x == 0 && atomicSub(&p.remaining[vi], 1) == 1) {
+                __threadfence_system();
+                *reinterpret_cast<volatile unsigned int*>(&p.done_flags[vi]) = p.epoch;
+            }
+        }
     }
 }
 
 // One fill launch: up to kChunk view records and their tile prefixes, passed by value.
 constexpr int kChunk = 112;
 struct FillChunk {
-    NoAllocView rec[kChunk];
+    ViewRecord rec[kChunk];
     int32_t prefix[kChunk];
     int32_t k0, n;       // first view slot, records in this chunk
     int32_t total;       // items of the whole call (written after the last view's prefix)
@@ -122,9 +114,9 @@ static_assert(sizeof(FillChunk) <= 32000, "kernel parameter space");
 
 __global__ void fill_scratch(const __grid_constant__ FillChunk c, unsigned char* scratch)
 {
-    constexpr int kWords = sizeof(NoAllocView) / 8;
+    constexpr int kWords = sizeof(ViewRecord) / 8;
     const uint64_t* src = reinterpret_cast<const uint64_t*>(&c.rec[0]);
-    uint64_t* dst = reinterpret_cast<uint64_t*>(scratch + kViewsOffset + sizeof(NoAllocView) * c.k0);
+    uint64_t* dst = reinterpret_cast<uint64_t*>(scratch + kViewsOffset + sizeof(ViewRecord) * c.k0);
     for (int i = threadIdx.x; i < c.n * kWords; i += blockDim.x) dst[i] = src[i];
     int32_t* pf = reinterpret_cast<int32_t*>(scratch + kPrefixOffset);
     for (int i = threadIdx.x; i < c.n; i += blockDim.x) pf[c.k0 + i] = c.prefix[i];
@@ -135,9 +127,9 @@ __global__ void fill_scratch(const __grid_constant__ FillChunk c, unsigned char*
 }
 
 template <int SD, bool ROLLED>
-cudaError_t launch_variant(const NoAllocLaunch& l, int device, cudaStream_t stream)
+cudaError_t launch_variant(const ViewsLaunch& l, int device, cudaStream_t stream)
 {
-    const auto kernel = render_views_noalloc<SD, ROLLED>;
+    const auto kernel = render_views<SD, ROLLED>;
     const size_t smem = pix::smem_bytes(SD, l.live_words);
     cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int sms = 0, per_sm = 0;
@@ -148,20 +140,6 @@ cudaError_t launch_variant(const NoAllocLaunch& l, int device, cudaStream_t stre
     grid = std::max(1, std::min(grid, l.n_items));
     kernel<<<grid, kThreads, smem, stream>>>(l);
     return cudaGetLastError();
-}
-
-cudaError_t dispatch(const NoAllocLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
-{
-    switch (stack_class) {
-        case 4: return rolled ? launch_variant<4, true>(l, device, stream) : launch_variant<4, false>(l, device, stream);
-        case 8: return rolled ? launch_variant<8, true>(l, device, stream) : launch_variant<8, false>(l, device, stream);
-        case 12:
-            return rolled ? launch_variant<12, true>(l, device, stream) : launch_variant<12, false>(l, device, stream);
-        case 16:
-            return rolled ? launch_variant<16, true>(l, device, stream) : launch_variant<16, false>(l, device, stream);
-        default:
-            return rolled ? launch_variant<32, true>(l, device, stream) : launch_variant<32, false>(l, device, stream);
-    }
 }
 
 // Address of the scratch array on each device, looked up on the first call there.
@@ -186,6 +164,21 @@ double view_cost(const csg_view& v)
 }
 
 }  // namespace
+
+cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
+{
+    switch (stack_class) {
+        case 4: return rolled ? launch_variant<4, true>(l, device, stream) : launch_variant<4, false>(l, device, stream);
+        case 8: return rolled ? launch_variant<8, true>(l, device, stream) : launch_variant<8, false>(l, device, stream);
+        case 12:
+            return rolled ? launch_variant<12, true>(l, device, stream) : launch_variant<12, false>(l, device, stream);
+        case 16:
+            return rolled ? launch_variant<16, true>(l, device, stream) : launch_variant<16, false>(l, device, stream);
+        default:
+            return rolled ? launch_variant<32, true>(l, device, stream) : launch_variant<32, false>(l, device, stream);
+    }
+}
+
 }  // namespace csgrt
 
 extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream)
@@ -195,7 +188,7 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
     if (n_views > kMaxViews) return CSG_E_CAPACITY;
     if (warp_tile_w == 0) warp_tile_w = 8;
     if (warp_tile_w != 4 && warp_tile_w != 8 && warp_tile_w != 16 && warp_tile_w != 32) return CSG_E_ARG;
-    const int tw = warp_tile_w, th = 32 / warp_tile_w;
+    const int tw = warp_tile_w;
     int32_t sd = 4, live = 1;
     bool rolled = false;
     for (int32_t i = 0; i < n_views; ++i) {
@@ -223,7 +216,7 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
     for (int32_t k = 0; k < n_views; ++k) {
         const csg_view& v = views[order[k]];
         prefix[k] = static_cast<int32_t>(total);
-        total += (long long)((v.w + 2 * tw - 1) / (2 * tw)) * ((v.h + 2 * th - 1) / (2 * th));
+        total += view_tiles(v.w, v.h, tw);
         if (total > INT_MAX) return CSG_E_CAPACITY;
     }
     prefix[n_views] = static_cast<int32_t>(total);
@@ -235,22 +228,10 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
         const int32_t n = std::min<int32_t>(kChunk, n_views - k0);
         for (int32_t j = 0; j < n; ++j) {
             const csg_view& v = views[order[k0 + j]];
-            NoAllocView& r = c.rec[j];
-            r = NoAllocView{};
-            r.view.scene = v.scene->dev;
-            std::memcpy(r.view.cam.v, &v.cam, sizeof(r.view.cam.v));
-            r.view.light[0] = v.light_dir[0];
-            r.view.light[1] = v.light_dir[1];
-            r.view.light[2] = v.light_dir[2];
-            r.view.w = v.w;
-            r.view.h = v.h;
-            r.view.out.rgba8 = v.out.rgba8;
-            r.view.out.rgba32f = reinterpret_cast<float4*>(v.out.rgba32f);
-            r.view.out.t = v.out.t;
-            r.view.out.prim = v.out.prim;
-            r.view.out.normal = v.out.normal;
-            r.status = v.scene->status;
-            r.tiles_x = (v.w + 2 * tw - 1) / (2 * tw);
+            const Planes out{v.out.rgba8, reinterpret_cast<float4*>(v.out.rgba32f), v.out.t, v.out.prim,
+                             v.out.normal};
+            make_view_record(v.scene->dev, v.scene->status, reinterpret_cast<const float*>(&v.cam), v.light_dir,
+                             v.w, v.h, out, tw, c.rec[j]);
             c.prefix[j] = prefix[k0 + j];
         }
         c.k0 = k0;
@@ -261,14 +242,17 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
         if (cudaGetLastError() != cudaSuccess) return CSG_E_CUDA;
     }
 
-    NoAllocLaunch l;
-    l.views = reinterpret_cast<const NoAllocView*>(scratch + kViewsOffset);
+    ViewsLaunch l;
+    l.views = reinterpret_cast<const ViewRecord*>(scratch + kViewsOffset);
     l.prefix = reinterpret_cast<const int32_t*>(scratch + kPrefixOffset);
     l.counter = reinterpret_cast<int*>(scratch);
     l.n_views = n_views;
     l.n_items = static_cast<int32_t>(total);
-    l.tw_log2 = tw == 4 ? 2 : tw == 8 ? 3 : tw == 16 ? 4 : 5;
+    l.tw_log2 = tile_log2(tw);
     l.live_words = live;
     l.iter_cap = kIterCap;
-    return dispatch(l, stack_class_for_depth(sd), rolled, device, st) == cudaSuccess ? CSG_OK : CSG_E_CUDA;
+    l.remaining = nullptr;
+    l.done_flags = nullptr;
+    l.epoch = 0;
+    return launch_views(l, stack_class_for_depth(sd), rolled, device, st) == cudaSuccess ? CSG_OK : CSG_E_CUDA;
 }

@@ -65,7 +65,14 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err);
 //                     child >= 0 is a BVH node and child < 0 is leaf ~prim (type valid)
 // ---------------------------------------------------------------------------------
 constexpr int kKidsPerNode = 5;
-constexpr int kLiveWordsMax = 32;  // live-leaf mask: at most 32 words (1024 bits) per ray
+// Live-leaf mask: at most CSG_LIVE_WORDS_MAX words per ray (32: 1024 bits; 64 is the
+// largest the one-register word summary can index).  A build-time tuning knob: more words
+// keep one bit per leaf on larger trees at the cost of shared memory per block.
+#ifndef CSG_LIVE_WORDS_MAX
+#define CSG_LIVE_WORDS_MAX 32
+#endif
+constexpr int kLiveWordsMax = CSG_LIVE_WORDS_MAX;
+static_assert(kLiveWordsMax >= 1 && kLiveWordsMax <= 64, "live-mask words");
 
 struct DeviceScene {
     const int4* topo = nullptr;

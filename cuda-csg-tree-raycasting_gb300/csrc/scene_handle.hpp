@@ -13,3 +13,13 @@ struct csg_scene {
     unsigned long long* status = nullptr;   // rays stopped at the traversal iteration cap
     int device = 0;
 };
+
+namespace csgrt {
+
+// Byte offsets of a scene's arrays inside its one device allocation (16-byte aligned).
+struct SceneLayout {
+    size_t topo, kids, geo, color, bvh, status, total;
+};
+SceneLayout scene_layout(size_t n_nodes, size_t n_prims, size_t n_kids_f4, size_t n_bvh_f4);
+
+}  // namespace csgrt

@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "scene.hpp"
@@ -440,12 +441,14 @@ struct SmemStacks {
 // returns Miss and when an operator child's box culls (its leaves' boxes are nested in
 // it, so they cull too).  The mask lives in shared memory, word k of a lane at
 // w[k * nt]; `sum` has bit k set while word k is non-zero.
+using live_sum_t = std::conditional<(kLiveWordsMax > 32), unsigned long long, uint32_t>::type;
+
 struct LiveMask {
     uint32_t* w;
     int nt;
     int shift;
     int words;
-    uint32_t sum;
+    live_sum_t sum;
 
     __device__ __forceinline__ uint32_t& word(int k) { return w[k * nt]; }
     __device__ __forceinline__ void fill(int n_groups)
@@ -455,7 +458,7 @@ struct LiveMask {
             const int rem = n_groups - 32 * k;
             const uint32_t v = rem >= 32 ? 0xffffffffu : (rem <= 0 ? 0u : ((1u << rem) - 1u));
             word(k) = v;
-            if (v) sum |= 1u << k;
+            if (v) sum |= (live_sum_t)1 << k;
         }
     }
     __device__ __forceinline__ void clear_all()
@@ -467,7 +470,7 @@ struct LiveMask {
     {
         const int g = leaf >> shift;
         word(g >> 5) |= 1u << (g & 31);
-        sum |= 1u << (g >> 5);
+        sum |= (live_sum_t)1 << (g >> 5);
     }
     __device__ __forceinline__ bool any(int lo, int hi)
     {
@@ -476,7 +479,7 @@ struct LiveMask {
         const uint32_t ma = 0xffffffffu << (a & 31);
         const uint32_t mb = 0xffffffffu >> (31 - (b & 31));
         if (wa == wb) return ((sum >> wa) & 1u) && (word(wa) & ma & mb);
-        const uint32_t mid = (uint32_t)(((1ull << wb) - 1ull) & ~((1ull << (wa + 1)) - 1ull));
+        const live_sum_t mid = (live_sum_t)(((1ull << wb) - 1ull) & ~((1ull << (wa + 1)) - 1ull));
         if (sum & mid) return true;
         if (((sum >> wa) & 1u) && (word(wa) & ma)) return true;
         return ((sum >> wb) & 1u) && (word(wb) & mb);
@@ -485,7 +488,7 @@ struct LiveMask {
     {
         const uint32_t v = word(k) & ~m;
         word(k) = v;
-        if (!v) sum &= ~(1u << k);
+        if (!v) sum &= ~((live_sum_t)1 << k);
     }
     __device__ __forceinline__ void clear_leaf(int leaf)
     {

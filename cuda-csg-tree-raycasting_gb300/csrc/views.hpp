@@ -1,0 +1,76 @@
+// Launch interface of the view-table kernel (noalloc.cu): many views of many scenes in one
+// persistent launch whose work items are found by a binary search of a per-view tile
+// prefix, so its tables are O(views).  Used by csg_render_views_noalloc (tables in a
+// fixed device array) and by the render server (tables per in-flight batch).
+#pragma once
+
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "render.hpp"
+
+namespace csgrt {
+
+// One view in the device table.
+struct ViewRecord {
+    ViewParams view;
+    unsigned long long* status;  // the scene's capped-ray counter
+    int32_t tiles_x;              // block tiles per row
+    int32_t host_out;             // an output plane is host memory (system-scope fences)
+};
+static_assert(sizeof(ViewRecord) % 8 == 0, "view record alignment");
+
+struct ViewsLaunch {
+    const ViewRecord* views;
+    const int32_t* prefix;  // prefix[v] = first item of view v; prefix[n_views] = n_items
+    int* counter;           // work counter: must be zero when the kernel starts
+    int32_t n_views;
+    int32_t n_items;
+    int32_t tw_log2;        // warp tile width 1 << tw_log2, height 32 >> tw_log2
+    int32_t live_words;     // max over the views
+    uint32_t iter_cap;
+    // Optional per-view completion (null: none).  remaining[v] starts at view v's tile
+    // count; the block that renders a view's last tile stores `epoch` to done_flags[v], a
+    // host-mapped word the host polls.  Every block fences its writes before counting its
+    // tile (system-wide if the view writes host memory), and the last one fences again
+    // system-wide before the flag.
+    int* remaining;
+    unsigned int* done_flags;
+    unsigned int epoch;
+};
+
+// Block tiles of a w x h view for warp tile width tw (a block is 2x2 warp tiles).
+inline int64_t view_tiles(int32_t w, int32_t h, int tw)
+{
+    const int th = 32 / tw;
+    return (int64_t)((w + 2 * tw - 1) / (2 * tw)) * ((h + 2 * th - 1) / (2 * th));
+}
+
+inline int tile_log2(int tw)
+{
+    return tw == 4 ? 2 : tw == 8 ? 3 : tw == 16 ? 4 : 5;
+}
+
+inline void make_view_record(const DeviceScene& scene, unsigned long long* status, const float cam[15],
+                             const float light[3], int32_t w, int32_t h, const Planes& out, int tw, ViewRecord& r)
+{
+    r = ViewRecord{};
+    r.view.scene = scene;
+    std::memcpy(r.view.cam.v, cam, sizeof(r.view.cam.v));
+    r.view.light[0] = light[0];
+    r.view.light[1] = light[1];
+    r.view.light[2] = light[2];
+    r.view.w = w;
+    r.view.h = h;
+    r.view.out = out;
+    r.status = status;
+    r.tiles_x = (w + 2 * tw - 1) / (2 * tw);
+    r.host_out = 0;
+}
+
+// Enqueues the view-table kernel variant for (stack_class, rolled) on `stream`, with a
+// grid that fills `device` once.
+cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream);
+
+}  // namespace csgrt

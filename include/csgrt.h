@@ -179,6 +179,80 @@ int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
 #define CSG_NOALLOC_MAX_VIEWS 4096
 int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream);
 
+/* ---- render server: continuous batching of render requests ---------------------------
+ * No counterpart in the reference (one interactive view per frame).  A server owns a
+ * pool of scenes, made resident on the device on first use and evicted least recently
+ * used when the device-memory budget (resident scenes + in-flight outputs) would be
+ * exceeded.  Requests queue as they arrive; a dispatcher thread admits them, as slots
+ * (batches in flight, one stream each) and memory free up, into batches rendered by the
+ * persistent view-table kernel, so requests that arrive while others run start on a free
+ * slot and overlap the running work on the device.  Each request's planes are the bytes
+ * csg_render_planes writes for it alone. */
+typedef struct csg_server csg_server;
+
+#define CSG_PLANE_RGBA8 1
+#define CSG_PLANE_T 2
+#define CSG_PLANE_PRIM 4
+#define CSG_PLANE_NORMAL 8
+#define CSG_PLANE_RGBA32F 16
+
+typedef struct csg_server_config {
+    uint64_t hbm_budget;      /* bytes for resident scenes + outputs in flight (0: 40 GiB) */
+    int32_t slots;            /* batches in flight, one stream each (0: 4; at most 16) */
+    int32_t max_batch_views;  /* views per batch (0: 256; at most 4096) */
+    int32_t warp_tile_w;      /* 4, 8, 16 or 32 (0: 8) */
+    int32_t planes;           /* CSG_PLANE_* bits rendered per request (0: RGBA8) */
+    int32_t keep_results;     /* 1: device planes stay until csg_server_release; 0: freed when done */
+    int32_t order;            /* views of a batch: 0 in arrival order, 1 longest first */
+} csg_server_config;
+
+#define CSG_REQ_ALONE 1       /* render with its own single-view launch (the unbatched form) */
+
+typedef struct csg_request {
+    int32_t scene;            /* id from csg_server_add_scene */
+    int32_t flags;            /* CSG_REQ_* */
+    csg_camera cam;
+    float light_dir[3];
+    int32_t w, h;
+    void* host_rgba8;         /* optional: the RGBA8 plane is also copied here (pinned memory
+                                 recommended), before the request counts as done */
+} csg_request;
+
+typedef struct csg_result {
+    int32_t status;           /* CSG_OK, or why this request failed (CSG_E_BUDGET: it can never fit) */
+    int32_t batch_views;      /* views in the launch that rendered it */
+    double t_arrive, t_launch, t_done;  /* seconds on the server's clock (csg_server_clock) */
+    csg_planes planes;        /* device planes (valid until released, with keep_results) */
+} csg_result;
+
+typedef struct csg_server_stats {
+    uint64_t budget, scene_bytes, output_bytes, peak_bytes;
+    int64_t requests_done, batches, evictions, rejected;
+    int32_t scenes, resident_scenes, slots_busy, pending;
+} csg_server_stats;
+
+int csg_server_create(const csg_server_config* cfg, csg_server** out);
+/* Finishes every queued and in-flight request, then frees everything. */
+int csg_server_destroy(csg_server* server);
+/* Parses a scene (errors as csg_scene_create) into the pool; resident on first use. */
+int csg_server_add_scene(csg_server* server, const char* text, size_t len, int32_t* id, char* err, size_t errlen);
+/* Makes a scene resident now (CSG_E_BUDGET if it cannot fit). */
+int csg_server_preload(csg_server* server, int32_t id);
+/* Queues a request; returns at once with its ticket. */
+int csg_server_submit(csg_server* server, const csg_request* req, int64_t* ticket);
+/* Waits up to timeout_s (< 0: forever) for a request; CSG_E_TIMEOUT if not done by then. */
+int csg_server_wait(csg_server* server, int64_t ticket, double timeout_s, csg_result* out);
+/* Forgets a finished request and frees its device planes. */
+int csg_server_release(csg_server* server, int64_t ticket);
+/* Open-loop replay: submits reqs[i] at arrival_s[i] seconds after the call starts, waits
+ * for all, fills results (t_arrive = the scheduled arrival) and the wall time from the
+ * start to the last completion.  tickets (optional) receives the tickets, which the caller
+ * then releases; without it the requests are released here. */
+int csg_server_replay(csg_server* server, const csg_request* reqs, const double* arrival_s, int32_t n,
+                      csg_result* results, int64_t* tickets, double* wall_s);
+int csg_server_stats_get(csg_server* server, csg_server_stats* out);
+double csg_server_clock(const csg_server* server);
+
 /* ---- misc ---------------------------------------------------------------------------- */
 /* Diagnostic: tan(fov / 2) as the device's ray generation computes it (RaycastingKernels.cu
  * :15-16 evaluates tan on the device).  Synchronous.  For checkers that restate the ray

@@ -64,3 +64,17 @@ def test_render_rejects_bad_arguments_without_gpu(csg):
     assert lib.csg_scene_destroy(None) == csg.CSG_E_ARG
     out = ctypes.c_void_p()
     assert lib.csg_scene_create(None, 5, ctypes.byref(out), None, 0) == csg.CSG_E_ARG
+
+
+def test_server_rejects_bad_configs_without_gpu(csg):
+    lib = csg.lib()
+    h = ctypes.c_void_p()
+    for bad in (dict(slots=17), dict(slots=-1), dict(max_batch_views=5000), dict(warp_tile_w=6), dict(planes=64),
+                dict(order=2)):
+        cfg = csg.csg_server_config()
+        for k, v in bad.items():
+            setattr(cfg, k, v)
+        assert lib.csg_server_create(ctypes.byref(cfg), ctypes.byref(h)) == csg.CSG_E_ARG, bad
+    assert lib.csg_server_create(None, None) == csg.CSG_E_ARG
+    assert lib.csg_server_submit(None, None, None) == csg.CSG_E_ARG
+    assert lib.csg_server_release(None, 1) == csg.CSG_E_ARG
