@@ -282,7 +282,11 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err)
     return kOk;
 }
 
-bool use_prepass(int32_t n_prims) { return n_prims >= 8; }
+// Build-time tuning knob: smallest tree (in primitives) that runs the liveness pre-pass.
+#ifndef CSG_PREPASS_MIN_PRIMS
+#define CSG_PREPASS_MIN_PRIMS 8
+#endif
+bool use_prepass(int32_t n_prims) { return n_prims >= CSG_PREPASS_MIN_PRIMS; }
 
 bool use_rolled(const HostTree& tree)
 {

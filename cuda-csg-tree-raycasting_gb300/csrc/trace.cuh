@@ -149,15 +149,19 @@ __device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float
 // isBVHNodeHit (RaycastingKernels.cu:718-756): slab test with six divisions.
 // Returns true when the box must be entered (a cull sets hit = Miss in the caller).
 // Out of line: taken only by the rare rays the certified test below cannot decide, and
-// its six IEEE divisions are a lot of code to inline at every call site.
-static __device__ __noinline__ bool box_hit_exact(const Ray& r, float4 lo, float4 hi, float tmin)
+// its six IEEE divisions are a lot of code to inline at every call site.  Everything is
+// passed by value: a reference argument would force the caller's ray into local memory
+// on every test, taken or not.
+static __device__ __noinline__ bool box_hit_exact(float ox, float oy, float oz, float dx, float dy, float dz,
+                                                  float lox, float loy, float loz, float hix, float hiy,
+                                                  float hiz, float tmin)
 {
-    const float t1 = __fdiv_rn(__fsub_rn(lo.x, r.o.x), r.d.x);
-    const float t2 = __fdiv_rn(__fsub_rn(hi.x, r.o.x), r.d.x);
-    const float t3 = __fdiv_rn(__fsub_rn(lo.y, r.o.y), r.d.y);
-    const float t4 = __fdiv_rn(__fsub_rn(hi.y, r.o.y), r.d.y);
-    const float t5 = __fdiv_rn(__fsub_rn(lo.z, r.o.z), r.d.z);
-    const float t6 = __fdiv_rn(__fsub_rn(hi.z, r.o.z), r.d.z);
+    const float t1 = __fdiv_rn(__fsub_rn(lox, ox), dx);
+    const float t2 = __fdiv_rn(__fsub_rn(hix, ox), dx);
+    const float t3 = __fdiv_rn(__fsub_rn(loy, oy), dy);
+    const float t4 = __fdiv_rn(__fsub_rn(hiy, oy), dy);
+    const float t5 = __fdiv_rn(__fsub_rn(loz, oz), dz);
+    const float t6 = __fdiv_rn(__fsub_rn(hiz, oz), dz);
     const float tmn = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
     const float tmx = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
     if (tmx < 0.0f) return false;
@@ -178,7 +182,8 @@ static __device__ __noinline__ bool box_hit_exact(const Ray& r, float4 lo, float
 // overflows) always uses divisions (Ray::exact).
 __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, float tmin)
 {
-    if (r.exact) return box_hit_exact(r, lo, hi, tmin);
+    if (r.exact)
+        return box_hit_exact(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tmin);
     const float t1 = __fmul_rn(__fsub_rn(lo.x, r.o.x), r.inv.x);
     const float t2 = __fmul_rn(__fsub_rn(hi.x, r.o.x), r.inv.x);
     const float t3 = __fmul_rn(__fsub_rn(lo.y, r.o.y), r.inv.y);
@@ -193,7 +198,8 @@ __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, floa
     const bool sure = (fabsf(__fsub_rn(tmn, tmx)) > kRel * (an + ax)) &&
                       (fabsf(__fsub_rn(tmx, tmin)) > kRel * ax) && (an > kTiny) && (ax > kTiny) &&
                       (ax < 3.0e38f) && (an < 3.0e38f);
-    if (!sure) return box_hit_exact(r, lo, hi, tmin);
+    if (!sure)
+        return box_hit_exact(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tmin);
     if (tmx < 0.0f) return false;
     if (tmn > tmx) return false;
     return tmx > tmin;
@@ -514,10 +520,14 @@ constexpr int kWarpStack = 64;
 // Liveness at tmin = 0 of one leaf whose own box already passed at tmin = 0: a cube's box
 // is the cube (the cube test is the same slab test), so it is live; a sphere or cylinder
 // is live when its primitive test at tmin = 0 is not a Miss.
+// Build-time tuning knob: 0 skips the primitive test (box test only) in the pre-pass.
+#ifndef CSG_PREPASS_PRIM_TEST
+#define CSG_PREPASS_PRIM_TEST 1
+#endif
 __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* __restrict__ geo, int prim,
                                                   int type)
 {
-    if (type == kCube) return true;
+    if (type == kCube || !CSG_PREPASS_PRIM_TEST) return true;
     Hit h = hit_default();
     const float4 g0 = __ldg(&geo[2 * prim]);
     if (type == kSphere) {
