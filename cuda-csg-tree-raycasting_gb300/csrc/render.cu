@@ -65,7 +65,7 @@ cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
     return p.view.scene.rolled ? launch_variant<SD, true>(p, stream) : launch_variant<SD, false>(p, stream);
 }
 
-__global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fdiv_rn(fov, 2.0f)); }
+__global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fmul_rn(fov, 0.5f)); }
 
 }  // namespace
 

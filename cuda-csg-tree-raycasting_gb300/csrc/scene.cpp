@@ -288,9 +288,14 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err)
 #endif
 bool use_prepass(int32_t n_prims) { return n_prims >= CSG_PREPASS_MIN_PRIMS; }
 
+// Build-time tuning knob: trees with cylinders and more primitives than this use the
+// rolled kernel variant.
+#ifndef CSG_ROLLED_MIN_PRIMS
+#define CSG_ROLLED_MIN_PRIMS 8
+#endif
 bool use_rolled(const HostTree& tree)
 {
-    if (tree.prims.size() <= 8) return false;
+    if (tree.prims.size() <= (size_t)CSG_ROLLED_MIN_PRIMS) return false;
     for (const RefNode& n : tree.nodes)
         if (n.type == kCylinder) return true;
     return false;

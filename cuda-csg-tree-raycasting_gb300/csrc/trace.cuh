@@ -9,7 +9,8 @@
 // RaycastingKernels.cu), where a sum or difference with a product operand becomes one
 // fused multiply-add: dot(a, b) = fma(a.z, b.z, fma(a.x, b.x, a.y * b.y)),
 // origin + t * dir = fma(t, dir, origin), c - r * r = fma(-r, r, c), and so on.
-// Divisions and square roots are IEEE (the reference's default -prec-div/-prec-sqrt).
+// Divisions and square roots are IEEE (the reference's default -prec-div/-prec-sqrt);
+// a halving x / 2 is computed as x * 0.5, the same correctly rounded value.
 // Results -- hit, primitive, t, normal -- are therefore bit-identical to the
 // reference kernel's on the same camera and scene bytes.
 #pragma once
@@ -130,7 +131,7 @@ __device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float
 {
     const float u = __fdiv_rn(__fadd_rn((float)x, 0.5f), __fsub_rn(width, 1.0f));
     const float v = __fdiv_rn(__fadd_rn((float)y, 0.5f), __fsub_rn(height, 1.0f));
-    const float thf = tanf(__fdiv_rn(cam[5], 2.0f));
+    const float thf = tanf(__fmul_rn(cam[5], 0.5f));
     const float nx = __fmul_rn(__fmul_rn(__fmaf_rn(2.0f, u, -1.0f), __fdiv_rn(width, height)), thf);
     const float ny = __fmul_rn(__fmaf_rn(-2.0f, v, 1.0f), thf);
     V3 d;
@@ -289,7 +290,7 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     const float rad = g0.w, hgt = g1.x;
     const V3 V = mk(g1.y, g1.z, g1.w);
     const V3 cen = mk(g0.x, g0.y, g0.z);
-    const float h2 = __fdiv_rn(hgt, 2.0f);
+    const float h2 = __fmul_rn(hgt, 0.5f);
     const V3 C = sub_scaled_unfused(cen, h2, V);
     const V3 OC = sub3(r.o, C);
     const float dV = dot_yx_z(r.d, V);
@@ -305,17 +306,19 @@ __device__ __forceinline__ void cylinder_hit(const Ray& r, float4 g0, float4 g1,
     const float m1 = __fmaf_rn(t1, dV, cH);
     const float m2 = __fmaf_rn(t2, dV, cH);
     if ((m1 < 0.0f && m2 < 0.0f) || (m1 > hgt && m2 > hgt)) return;
-    float temp = t1, m = m1;
-    bool skip = false;
-    int use = 0;
-    cylinder_caps(r, V, OC, cen, h2, hgt, m, temp, skip, use);
-    if (temp <= tmin || skip) {
-        temp = t2;
-        m = m2;
-        skip = false;
+    // The near root, then the far one, each possibly replaced by a cap; one copy of the cap
+    // code serves both.
+    float temp, m;
+    int use;
+#pragma unroll 1
+    for (int k = 0;; ++k) {
+        temp = k ? t2 : t1;
+        m = k ? m2 : m1;
+        bool skip = false;
         use = 0;
         cylinder_caps(r, V, OC, cen, h2, hgt, m, temp, skip, use);
-        if (temp <= tmin || skip) return;
+        if (!(temp <= tmin || skip)) break;
+        if (k == 1) return;
     }
     h.t = temp;
     V3 n;
@@ -333,7 +336,7 @@ __device__ __forceinline__ void cube_hit(const Ray& r, float4 g0, int32_t id, Hi
 {
     h.hit = kMiss;
     h.idx = id;
-    const float s2 = __fdiv_rn(g0.w, 2.0f);
+    const float s2 = __fmul_rn(g0.w, 0.5f);
     const V3 C = mk(g0.x, g0.y, g0.z);
     const float t1 = __fdiv_rn(__fsub_rn(__fsub_rn(C.x, s2), r.o.x), r.d.x);
     const float t2 = __fdiv_rn(__fsub_rn(__fadd_rn(C.x, s2), r.o.x), r.d.x);
@@ -883,7 +886,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     } else if (h.type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * h.idx + 1]);
         const V3 V = mk(g1.y, g1.z, g1.w);
-        const V3 C = sub_scaled(cen, __fdiv_rn(g1.x, 2.0f), V);
+        const V3 C = sub_scaled(cen, __fmul_rn(g1.x, 0.5f), V);
         const V3 OC = sub3(ray.o, C);
         if (h.hit & kFlag1) {
             N = neg3(V);
@@ -896,7 +899,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     } else {
         const V3 PC = sub3(P, cen);
         const float bias = 1.00001f;  // `float bias = 1.00001;` rounds to the same float
-        const float hs = __fdiv_rn(g0.w, 2.0f);
+        const float hs = __fmul_rn(g0.w, 0.5f);
         const V3 n = mk((float)(int)__fmul_rn(__fdiv_rn(PC.x, hs), bias),
                         (float)(int)__fmul_rn(__fdiv_rn(PC.y, hs), bias),
                         (float)(int)__fmul_rn(__fdiv_rn(PC.z, hs), bias));
