@@ -56,12 +56,12 @@ class Oracle:
         L.orc_parse.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _vp, _i, _vp, _i,
                                 ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.c_char_p, ctypes.c_size_t]
         L.orc_parse.restype = _i
-        for name in ("orc_render_ieee", "orc_render_fma"):
+        for name in ("orc_render_ieee", "orc_render_fma", "orc_render_f64"):
             fn = getattr(L, name)
             fn.argtypes = [_vp, _i, _vp, _i, _vp, _f, _vp, _i, _i, _i, _i, _i,
                            _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]
             fn.restype = _i
-        for name in ("orc_render_list_ieee", "orc_render_list_fma"):
+        for name in ("orc_render_list_ieee", "orc_render_list_fma", "orc_render_list_f64"):
             fn = getattr(L, name)
             fn.argtypes = [_vp, _i, _vp, _i, _vp, _f, _vp, _i, _i, _vp, ctypes.c_int64, _i,
                            _vp, _vp, _vp, _vp, _vp, _vp]
@@ -145,7 +145,7 @@ class Oracle:
         if counts:
             out["counts"] = np.zeros(n, COUNTS_DTYPE)
         y0, y1 = rows if rows is not None else (0, h)
-        fn = self.lib.orc_render_ieee if mode == "ieee" else self.lib.orc_render_fma
+        fn = {"ieee": self.lib.orc_render_ieee, "fma": self.lib.orc_render_fma, "f64": self.lib.orc_render_f64}[mode]
         capped = fn(_ptr(nodes), len(nodes), _ptr(prims), len(prims), _ptr(cam), thf, _ptr(light),
                     w, h, y0, y1, nthreads,
                     _ptr(out.get("hit")), _ptr(out.get("t")), _ptr(out.get("prim")),
@@ -167,7 +167,8 @@ class Oracle:
         out = {k: np.zeros(*shapes[k]) for k in want}
         if counts:
             out["counts"] = np.zeros(n, COUNTS_DTYPE)
-        fn = self.lib.orc_render_list_ieee if mode == "ieee" else self.lib.orc_render_list_fma
+        fn = {"ieee": self.lib.orc_render_list_ieee, "fma": self.lib.orc_render_list_fma,
+              "f64": self.lib.orc_render_list_f64}[mode]
         out["capped"] = fn(_ptr(nodes), len(nodes), _ptr(prims), len(prims), _ptr(cam), thf, _ptr(light), w, h,
                            _ptr(pix), n, nthreads, _ptr(out.get("hit")), _ptr(out.get("t")),
                            _ptr(out.get("prim")), _ptr(out.get("normal")), _ptr(out.get("rgba8")),

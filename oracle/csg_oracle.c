@@ -429,7 +429,7 @@ float orc_tan_half_fov(float fov)
 }
 
 /* ------------------------------------------------------------------------------------
- * Render core, two arithmetic modes.
+ * Render core, three arithmetic modes.
  * ---------------------------------------------------------------------------------- */
 /* FP32 operations of the reference source on the path a ray executes: every +, -, *,
  * /, sqrt, min, max, pow, tan counts 1 (as written in the reference, so a*b+c is 2);
@@ -447,4 +447,12 @@ static __thread uint64_t orc_flop_counter;
 #define ORC_SUFFIX(name) name##_fma
 #include "csg_oracle_render.inc"
 #undef ORC_FMA
+#undef ORC_SUFFIX
+
+#define ORC_FMA 0
+#define ORC_F64 1
+#define ORC_SUFFIX(name) name##_f64
+#include "csg_oracle_render.inc"
+#undef ORC_FMA
+#undef ORC_F64
 #undef ORC_SUFFIX

@@ -10,6 +10,8 @@
  * The "fma" mode restates the fused multiply-adds that nvcc's default contraction
  * (--fmad=true) forms in the reference CUDA kernel; it is pinned against that kernel's
  * own output on the GPU (tests/golden/ fixtures made by tests/golden/make_golden.py).
+ * The "f64" mode carries the same steps in double: the yardstick against which the
+ * FP32 results' errors are stated.
  *
  * Record layouts follow the reference byte for byte, so parse results can be compared
  * directly and fed to the reference kernel:
@@ -96,6 +98,17 @@ int orc_render_list_ieee(const orc_node* nodes, int n_nodes, const orc_prim* pri
                          int w, int h, const int64_t* pix, int64_t n_pix, int nthreads,
                          uint8_t* hit, float* t, int32_t* prim, float* normal3,
                          uint32_t* rgba8, orc_counts* counts);
+/* The same steps carried in double (the FP64 yardstick for error statements). */
+int orc_render_f64(const orc_node* nodes, int n_nodes, const orc_prim* prims, int n_prims,
+                   const float cam[15], float tan_half_fov, const float light[3],
+                   int w, int h, int y0, int y1, int nthreads,
+                   uint8_t* hit, float* t, int32_t* prim, float* normal3, float* pos3,
+                   float* rgba32f, uint32_t* rgba8, orc_counts* counts);
+int orc_render_list_f64(const orc_node* nodes, int n_nodes, const orc_prim* prims, int n_prims,
+                        const float cam[15], float tan_half_fov, const float light[3],
+                        int w, int h, const int64_t* pix, int64_t n_pix, int nthreads,
+                        uint8_t* hit, float* t, int32_t* prim, float* normal3,
+                        uint32_t* rgba8, orc_counts* counts);
 int orc_render_list_fma(const orc_node* nodes, int n_nodes, const orc_prim* prims, int n_prims,
                         const float cam[15], float tan_half_fov, const float light[3],
                         int w, int h, const int64_t* pix, int64_t n_pix, int nthreads,

@@ -122,3 +122,16 @@ def test_oracle_counts_and_fma_mode_are_consistent(oracle):
     assert (c["iters"] >= 1).all()
     assert c["aabb"].sum() >= 2 * c["iters"].astype(np.int64).sum() // 4
     assert (c["aabb"] % 2 == 0).all()
+
+
+def test_oracle_f64_states_the_fp32_error(oracle):
+    """The FP64 restatement agrees with the FP32 ("fma" = engine = reference kernel) results
+    on hit and primitive for these samples, and bounds their t and normal error."""
+    from csgrt import scenes
+    from report_f64_errors import error_stats
+    for text, view in ((scenes.config_scene_text(1), scenes.config_views(1)[0]),
+                       (scenes.config_scene_text(3, 0), scenes.config_views(3, 0)[0])):
+        s = error_stats(oracle, text, view, 320, 180, n_pix=1500)
+        assert s["hit_mismatch"] <= 2 and s["prim_mismatch"] <= 2, s
+        assert s["t_rel_p99"] < 1e-4 and s["normal_p99"] < 1e-3, s
+        assert s["rgba8_max"] <= 1, s
