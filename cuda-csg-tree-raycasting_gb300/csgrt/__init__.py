@@ -41,6 +41,7 @@ EXPORTED = [
     "csg_batch_get_info", "csg_batch_check", "csg_render_views_noalloc",
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
+    "csg_image_write",
 ]
 
 _vp = ctypes.c_void_p
@@ -167,6 +168,7 @@ def lib() -> ctypes.CDLL:
                                     ctypes.POINTER(ctypes.c_double)]
     L.csg_server_stats_get.argtypes = [_vp, ctypes.POINTER(csg_server_stats)]
     L.csg_server_clock.argtypes = [_vp]
+    L.csg_image_write.argtypes = [ctypes.c_char_p, _vp, _i32, _i32, _i32]
     L.csg_server_clock.restype = ctypes.c_double
     _LIB = L
     return L
@@ -183,6 +185,16 @@ def probe_fp32_peak() -> float:
     tf, ms = _f(), _f()
     check(lib().csg_probe_fp32_peak(ctypes.byref(tf), ctypes.byref(ms)))
     return tf.value
+
+
+def write_image(path, rgba8, w: int, h: int, fmt: str = "png"):
+    """Writes an RGBA8 frame (host array of w*h uint32/int32, row 0 on top) as PNG or PPM."""
+    import numpy as np
+    a = np.ascontiguousarray(np.asarray(rgba8).reshape(-1).view(np.uint32))
+    if a.size != w * h:
+        raise ValueError("frame size does not match w*h")
+    code = {"ppm": 0, "png": 1}[fmt]
+    check(lib().csg_image_write(str(path).encode(), a.ctypes.data, w, h, code))
 
 
 def status_string(code: int) -> str:

@@ -253,6 +253,14 @@ int csg_server_replay(csg_server* server, const csg_request* reqs, const double*
 int csg_server_stats_get(csg_server* server, csg_server_stats* out);
 double csg_server_clock(const csg_server* server);
 
+/* ---- headless image export ------------------------------------------------------------
+ * Replaces the reference's OpenGL display of the frame (RenderManager.cpp:69-84, no
+ * graphics stack here): writes a host RGBA8 frame (as csg_render produces it, row 0 on top)
+ * to `path` as binary PPM (RGB) or PNG (RGBA, uncompressed deflate).  Synchronous. */
+#define CSG_IMAGE_PPM 0
+#define CSG_IMAGE_PNG 1
+int csg_image_write(const char* path, const uint32_t* rgba8, int32_t w, int32_t h, int32_t format);
+
 /* ---- misc ---------------------------------------------------------------------------- */
 /* Diagnostic: tan(fov / 2) as the device's ray generation computes it (RaycastingKernels.cu
  * :15-16 evaluates tan on the device).  Synchronous.  For checkers that restate the ray
