@@ -209,7 +209,7 @@ def run_engine(args):
     text, view = load_scene_and_view(args.config)
     w, h = view.w, view.h
     rays = w * h
-    scene = csgrt.Scene(text)
+    scene = csgrt.Scene(text, exact_boxes=args.exact)
     cam = csgrt.Camera.from_floats(view.camera)
     stream = torch.cuda.current_stream()
     out = torch.empty(rays, dtype=torch.int32, device="cuda")
@@ -272,6 +272,8 @@ def run_engine(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": WORKLOADS[args.config], "config_index": args.config, "width": w, "height": h,
                    "rays_per_step": rays, "nodes": scene.info()["n_nodes"], "output": "RGBA8 device plane",
+                   "boxes": "exact (CSG_SCENE_EXACT_BOXES, not the reference's output)" if args.exact
+                   else "reference",
                    "l2": "flushed before every step by a 256 MiB device write (inside the timed region)",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "kernel_ms": {"mean": avg_launch_ms, "min": float(np.min(launch_ms)), "max": float(np.max(launch_ms))},
@@ -616,6 +618,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--exact", action="store_true",
+                    help="render with the optional exact-box mode (changes the output; for comparisons)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

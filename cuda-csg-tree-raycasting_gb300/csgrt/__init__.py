@@ -41,7 +41,7 @@ EXPORTED = [
     "csg_batch_get_info", "csg_batch_check", "csg_render_views_noalloc",
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
-    "csg_image_write",
+    "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex",
 ]
 
 _vp = ctypes.c_void_p
@@ -124,6 +124,11 @@ def lib() -> ctypes.CDLL:
     L.csg_scene_create.argtypes = [ctypes.c_char_p, ctypes.c_size_t, ctypes.POINTER(_vp), ctypes.c_char_p,
                                    ctypes.c_size_t]
     L.csg_scene_destroy.argtypes = [_vp]
+    L.csg_scene_create_ex.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _i32, ctypes.POINTER(_vp), ctypes.c_char_p,
+                                      ctypes.c_size_t]
+    L.csg_tree_parse_ex.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _i32, _vp, _i32, _vp, _i32,
+                                    ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                    ctypes.c_char_p, ctypes.c_size_t]
     L.csg_tree_parse.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _vp, _i32, _vp, _i32, ctypes.POINTER(_i32),
                                  ctypes.POINTER(_i32), ctypes.POINTER(_i32), ctypes.c_char_p, ctypes.c_size_t]
     L.csg_scene_get_info.argtypes = [_vp, ctypes.POINTER(csg_scene_info)]
@@ -206,20 +211,25 @@ def check(code: int, msg: str = ""):
         raise CsgError(code, msg or status_string(code))
 
 
-def parse_tree(text: str | bytes):
+CSG_SCENE_EXACT_BOXES = 1
+
+
+def parse_tree(text: str | bytes, exact_boxes: bool = False):
     """CSGTree::Parse on the host: (nodes, prims, op_depth) with nodes and prims as raw
-    bytes in the reference's 44-byte CSGNode / 48-byte Primitive layouts."""
+    bytes in the reference's 44-byte CSGNode / 48-byte Primitive layouts (boxes of the
+    exact-box mode with exact_boxes)."""
     data = text.encode() if isinstance(text, str) else bytes(text)
+    flags = CSG_SCENE_EXACT_BOXES if exact_boxes else 0
     nn, npr, dep = _i32(), _i32(), _i32()
     err = ctypes.create_string_buffer(512)
-    rc = lib().csg_tree_parse(data, len(data), None, 0, None, 0, ctypes.byref(nn), ctypes.byref(npr),
-                              ctypes.byref(dep), err, 512)
+    rc = lib().csg_tree_parse_ex(data, len(data), flags, None, 0, None, 0, ctypes.byref(nn), ctypes.byref(npr),
+                                 ctypes.byref(dep), err, 512)
     if rc != CSG_OK:
         raise CsgError(rc, err.value.decode(errors="replace"))
     nodes = np.zeros(nn.value * 44, np.uint8)
     prims = np.zeros(npr.value * 48, np.uint8)
-    check(lib().csg_tree_parse(data, len(data), nodes.ctypes.data, nn.value, prims.ctypes.data, npr.value,
-                               ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep), err, 512))
+    check(lib().csg_tree_parse_ex(data, len(data), flags, nodes.ctypes.data, nn.value, prims.ctypes.data,
+                                  npr.value, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep), err, 512))
     return nodes, prims, dep.value
 
 
@@ -288,11 +298,12 @@ def light_dir(polar=None, azimuth=None) -> np.ndarray:
 class Scene:
     """A parsed, device-resident CSG scene (opaque handle)."""
 
-    def __init__(self, text: str | bytes):
+    def __init__(self, text: str | bytes, exact_boxes: bool = False):
         data = text.encode() if isinstance(text, str) else bytes(text)
         h = _vp()
         err = ctypes.create_string_buffer(512)
-        rc = lib().csg_scene_create(data, len(data), ctypes.byref(h), err, 512)
+        rc = lib().csg_scene_create_ex(data, len(data), CSG_SCENE_EXACT_BOXES if exact_boxes else 0, ctypes.byref(h),
+                                       err, 512)
         if rc != CSG_OK:
             raise CsgError(rc, err.value.decode(errors="replace"))
         self.h = h

@@ -115,7 +115,13 @@ extern "C" {
 
 int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, size_t errlen)
 {
+    return csg_scene_create_ex(text, len, 0, out, err, errlen);
+}
+
+int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene** out, char* err, size_t errlen)
+{
     if (!out) return CSG_E_ARG;
+    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
     *out = nullptr;
     if (!text && len) return CSG_E_ARG;
     csg_scene* s = new (std::nothrow) csg_scene();
@@ -127,6 +133,7 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
         delete s;
         return rc;
     }
+    if (flags & CSG_SCENE_EXACT_BOXES) csgrt::use_exact_boxes(s->tree);
     csgrt::PackedScene pk;
     csgrt::pack_scene(s->tree, pk);
     const size_t n = s->tree.nodes.size(), np = s->tree.prims.size();
@@ -181,7 +188,16 @@ int csg_tree_parse(const char* text, size_t len, void* nodes44, int32_t max_node
                    int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
                    char* err, size_t errlen)
 {
+    return csg_tree_parse_ex(text, len, 0, nodes44, max_nodes, prims48, max_prims, n_nodes, n_prims, op_depth,
+                             err, errlen);
+}
+
+int csg_tree_parse_ex(const char* text, size_t len, int32_t flags, void* nodes44, int32_t max_nodes,
+                      void* prims48, int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
+                      char* err, size_t errlen)
+{
     if (!text && len) return CSG_E_ARG;
+    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
     csgrt::HostTree tree;
     std::string msg;
     const int rc = csgrt::parse_tree(std::string_view(text ? text : "", len), tree, msg);
@@ -189,6 +205,7 @@ int csg_tree_parse(const char* text, size_t len, void* nodes44, int32_t max_node
         copy_err(err, errlen, msg);
         return rc;
     }
+    if (flags & CSG_SCENE_EXACT_BOXES) csgrt::use_exact_boxes(tree);
     const int32_t nn = static_cast<int32_t>(tree.nodes.size());
     const int32_t np = static_cast<int32_t>(tree.prims.size());
     if (n_nodes) *n_nodes = nn;

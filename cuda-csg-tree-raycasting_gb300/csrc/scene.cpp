@@ -123,18 +123,50 @@ void leaf_box(RefNode& n, const RefPrim& p)
     n.maxx = hi[0]; n.maxy = hi[1]; n.maxz = hi[2];
 }
 
+// Exact-box mode: boxes that contain their primitive, instead of the reference's ±2r
+// sphere boxes and its cylinder boxes (BVHNode.cuh:19-49), which are not conservative
+// and cut hits.  A sphere gets ±r; a cylinder about axis V with half-height h/2 gets, per
+// axis, |V_k| h/2 + r sqrt(1 - V_k^2); both widened by 2^-12 of their size plus 1e-5 so
+// that the rounded hit points of the primitive tests stay inside; a cube keeps its own
+// box (already exact).  The oracle computes the same floats (oracle/csg_oracle.c,
+// orc_boxes_exact).
+void leaf_box_exact(RefNode& n, const RefPrim& p)
+{
+    if (n.type != kSphere && n.type != kCylinder) {
+        leaf_box(n, p);
+        return;
+    }
+    const float c[3] = {p.x, p.y, p.z};
+    float e[3];
+    if (n.type == kSphere) {
+        const float r = p.p[0];
+        for (int k = 0; k < 3; ++k) e[k] = r;
+    } else {
+        const float r = p.p[0], h2 = p.p[1] * 0.5f;
+        for (int k = 0; k < 3; ++k) {
+            const float v = p.p[2 + k];
+            const float s = 1.0f - v * v;
+            e[k] = std::fabs(v) * h2 + r * std::sqrt(s > 0.0f ? s : 0.0f);
+        }
+    }
+    for (int k = 0; k < 3; ++k) e[k] = e[k] + e[k] * 0.000244140625f + 1e-5f;
+    n.minx = c[0] - e[0]; n.miny = c[1] - e[1]; n.minz = c[2] - e[2];
+    n.maxx = c[0] + e[0]; n.maxy = c[1] + e[1]; n.maxz = c[2] + e[2];
+}
+
 // Operator boxes (BVHNode.cuh:54-63) with std::min / std::max semantics.
 inline float min_ref(float a, float b) { return (b < a) ? b : a; }
 inline float max_ref(float a, float b) { return (a < b) ? b : a; }
 
-void build_boxes(HostTree& t)
+void build_boxes(HostTree& t, bool exact = false)
 {
     // Children always follow their parent in preorder, so a reverse sweep visits every
     // child before its parent.
     for (int i = static_cast<int>(t.nodes.size()) - 1; i >= 0; --i) {
         RefNode& n = t.nodes[i];
         if (n.prim != -1) {
-            leaf_box(n, t.prims[n.prim]);
+            if (exact) leaf_box_exact(n, t.prims[n.prim]);
+            else leaf_box(n, t.prims[n.prim]);
         } else {
             const RefNode& l = t.nodes[n.left];
             const RefNode& r = t.nodes[n.right];
@@ -280,6 +312,11 @@ int parse_tree(std::string_view text, HostTree& out, std::string& err)
         }
     }
     return kOk;
+}
+
+void use_exact_boxes(HostTree& t)
+{
+    build_boxes(t, true);
 }
 
 // Build-time tuning knob: smallest tree (in primitives) that runs the liveness pre-pass.

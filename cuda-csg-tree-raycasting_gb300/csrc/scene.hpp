@@ -46,6 +46,8 @@ enum : int { kOk = 0, kErrParse = 1, kErrRange = 2, kErrCount = 3, kErrDepth = 7
 // CSGTree::Parse (CSGTree.cu:5-152) followed by ConstructBVH (CSGTree.cu:154-179).
 // Returns a status code; `err` receives the reference's exception text.
 int parse_tree(std::string_view text, HostTree& out, std::string& err);
+// Recomputes every box of a parsed tree in the exact-box mode (CSG_SCENE_EXACT_BOXES).
+void use_exact_boxes(HostTree& t);
 
 // ---------------------------------------------------------------------------------
 // Device layout (all arrays 16-byte aligned, one cudaMalloc):

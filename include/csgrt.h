@@ -79,6 +79,12 @@ typedef struct csg_planes {
  * *out is NULL and `err` (if given) holds the reference's message, e.g.
  * "Cannot parse - Unrecognized keyword: Spere". */
 int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, size_t errlen);
+/* Optional exact-box mode (no counterpart in the reference; off by default because it
+ * changes the output): sphere boxes ±r instead of ±2r and cylinder boxes that contain
+ * the cylinder (the reference's, BVHNode.cuh:34-49, cut hits), each widened by 2^-12 of
+ * its size plus 1e-5.  Cube and operator boxes as the reference builds them. */
+#define CSG_SCENE_EXACT_BOXES 1
+int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene** out, char* err, size_t errlen);
 /* Frees the scene's device memory (Raycaster::CleanUp, Raycaster.cu:36-44). */
 int csg_scene_destroy(csg_scene* scene);
 int csg_scene_get_info(const csg_scene* scene, csg_scene_info* info);
@@ -89,6 +95,10 @@ int csg_scene_get_info(const csg_scene* scene, csg_scene_info* info);
 int csg_tree_parse(const char* text, size_t len, void* nodes44, int32_t max_nodes, void* prims48,
                    int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
                    char* err, size_t errlen);
+/* csg_tree_parse with the csg_scene_create_ex flags (the boxes of the exact-box mode). */
+int csg_tree_parse_ex(const char* text, size_t len, int32_t flags, void* nodes44, int32_t max_nodes,
+                      void* prims48, int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
+                      char* err, size_t errlen);
 /* Copies the parsed tree out in the reference's own record layouts: 44-byte CSGNode
  * (CSGTree.cuh:15-34) and 48-byte Primitive (Primitives.h:29-40).  Pass NULL arrays to
  * query the counts. */

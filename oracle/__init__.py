@@ -67,6 +67,8 @@ class Oracle:
                            _vp, _vp, _vp, _vp, _vp, _vp]
             fn.restype = _i
         L.orc_tan_half_fov.argtypes = [_f]
+        L.orc_boxes_exact.argtypes = [_vp, _i, _vp]
+        L.orc_boxes_exact.restype = None
         L.orc_tan_half_fov.restype = _f
         for name, args in (("orc_camera_default", [_vp]),
                            ("orc_camera_set_position", [_vp, _f, _f, _f]),
@@ -80,7 +82,7 @@ class Oracle:
             getattr(L, name).restype = None
 
     # -- scene -------------------------------------------------------------------------
-    def parse(self, text: str | bytes, max_nodes: int | None = None):
+    def parse(self, text: str | bytes, max_nodes: int | None = None, exact_boxes: bool = False):
         data = text.encode() if isinstance(text, str) else text
         ntok = max(1, len(data.split()))
         max_nodes = max_nodes or ntok + 1
@@ -92,7 +94,10 @@ class Oracle:
                                 ctypes.byref(nn), ctypes.byref(npr), err, 512)
         if rc != 0:
             raise ParseError(rc, err.value.decode(errors="replace"))
-        return nodes[: nn.value].copy(), prims[: npr.value].copy()
+        nodes, prims = nodes[: nn.value].copy(), prims[: npr.value].copy()
+        if exact_boxes:
+            self.lib.orc_boxes_exact(_ptr(nodes), len(nodes), _ptr(prims))
+        return nodes, prims
 
     # -- camera / light ----------------------------------------------------------------
     def camera(self, position=None, rotation=None, fov_deg=None) -> np.ndarray:

@@ -142,6 +142,45 @@ static void leaf_box(orc_node* n, const orc_prim* p)
     n->maxx = hi[0]; n->maxy = hi[1]; n->maxz = hi[2];
 }
 
+/* Exact-box mode of the engine (csg_scene_create_ex with CSG_SCENE_EXACT_BOXES; no
+ * counterpart in the reference): a sphere gets +-r, a cylinder about axis V with
+ * half-height h/2 gets |V_k| h/2 + r sqrt(1 - V_k^2) per axis, both widened by 2^-12 of
+ * their size plus 1e-5; cubes keep the reference box.  Same float operations, in the same
+ * order, as the engine's scene compiler. */
+static void leaf_box_exact(orc_node* n, const orc_prim* p)
+{
+    if (n->type != ORC_SPHERE && n->type != ORC_CYLINDER) {
+        leaf_box(n, p);
+        return;
+    }
+    const float c[3] = {p->x, p->y, p->z};
+    float e[3];
+    if (n->type == ORC_SPHERE) {
+        for (int k = 0; k < 3; ++k) e[k] = p->p[0];
+    } else {
+        const float r = p->p[0], h2 = p->p[1] * 0.5f;
+        for (int k = 0; k < 3; ++k) {
+            const float v = p->p[2 + k];
+            const float s = 1.0f - v * v;
+            e[k] = fabsf(v) * h2 + r * sqrtf(s > 0.0f ? s : 0.0f);
+        }
+    }
+    for (int k = 0; k < 3; ++k) e[k] = e[k] + e[k] * 0.000244140625f + 1e-5f;
+    n->minx = c[0] - e[0]; n->miny = c[1] - e[1]; n->minz = c[2] - e[2];
+    n->maxx = c[0] + e[0]; n->maxy = c[1] + e[1]; n->maxz = c[2] + e[2];
+}
+
+static void merge_box(orc_node* n, const orc_node* l, const orc_node* r);
+
+void orc_boxes_exact(orc_node* nodes, int n_nodes, const orc_prim* prims)
+{
+    /* nodes are in preorder: a reverse sweep meets every child before its parent */
+    for (int i = n_nodes - 1; i >= 0; --i) {
+        if (nodes[i].prim != -1) leaf_box_exact(&nodes[i], &prims[nodes[i].prim]);
+        else merge_box(&nodes[i], &nodes[nodes[i].left], &nodes[nodes[i].right]);
+    }
+}
+
 /* std::min / std::max as the reference uses them (BVHNode.cuh:54-63):
  * min(a,b) = (b < a) ? b : a, max(a,b) = (a < b) ? b : a. */
 static float smin(float a, float b) { return (b < a) ? b : a; }

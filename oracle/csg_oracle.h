@@ -63,6 +63,9 @@ int orc_parse(const char* text, size_t len, orc_node* nodes, int max_nodes,
               orc_prim* prims, int max_prims, int* n_nodes, int* n_prims,
               char* err, size_t errlen);
 
+/* Recomputes the boxes of a parsed tree as the engine's exact-box mode does. */
+void orc_boxes_exact(orc_node* nodes, int n_nodes, const orc_prim* prims);
+
 void orc_camera_default(float cam[15]);
 void orc_camera_set_position(float cam[15], float x, float y, float z);
 void orc_camera_set_rotation(float cam[15], float pitch, float yaw);
