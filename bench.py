@@ -242,8 +242,11 @@ def run_engine(args):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    total_ms = t_start.elapsed_time(t_end)
+    # The K steps' own device time: the CUDA events bracket each render; the L2 flush
+    # between steps is outside them (its time is reported separately).
+    bracket_ms = t_start.elapsed_time(t_end)
     launch_ms = [a.elapsed_time(b) for a, b in ev]
+    total_ms = float(np.sum(launch_ms))
     if dist:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -274,9 +277,10 @@ def run_engine(args):
                    "rays_per_step": rays, "nodes": scene.info()["n_nodes"], "output": "RGBA8 device plane",
                    "boxes": "exact (CSG_SCENE_EXACT_BOXES, not the reference's output)" if args.exact
                    else "reference",
-                   "l2": "flushed before every step by a 256 MiB device write (inside the timed region)",
+                   "l2": "flushed before every step by a 256 MiB device write, between the steps' events",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "kernel_ms": {"mean": avg_launch_ms, "min": float(np.min(launch_ms)), "max": float(np.max(launch_ms))},
+        "flush_ms_per_step": round((bracket_ms - total_ms) / args.steps, 4),
         "gpu_launches": args.steps,
         "e2e": {"value": round(rays * e2e_steps / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 72,
                 "d2h_bytes_per_step": rays * 4,
@@ -391,7 +395,8 @@ def run_batch(args):
         torch.cuda.synchronize()
         if dist:
             dist.barrier()
-    total_ms = t0.elapsed_time(t1)
+    bracket_ms = t0.elapsed_time(t1)
+    total_ms = float(np.sum(b_ms))  # the steps' own events; the L2 flushes lie between them
     if dist:
         tt = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -443,8 +448,9 @@ def run_batch(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
         "config": {"workload": WORKLOADS[4], "config_index": 4, "views": len(views), "scenes": len(scene_objs),
                    "rays_per_step": rays, "output": "RGBA8 device planes",
-                   "l2": "flushed before every step by a 256 MiB device write (inside the timed region)",
+                   "l2": "flushed before every step by a 256 MiB device write, between the steps' events",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
+        "flush_ms_per_step": round((bracket_ms - total_ms) / args.steps, 4),
         "batch": {"warp_tile": [tile_w, 32 // tile_w], "tune_ms": round(tune_ms, 3), "grid": info["grid"],
                   "items": info["n_items"], "stack_class": info["stack_class"], "rolled": info["rolled"],
                   "kernel_ms": {"mean": float(np.mean(b_ms)), "min": float(np.min(b_ms))}},

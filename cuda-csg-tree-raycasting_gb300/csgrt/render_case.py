@@ -1,0 +1,83 @@
+"""Render one benchmark case through the C ABI: a configuration's view (optionally saved as
+PNG/PPM), or the first views of the batched workload as one csg_batch launch.  Small
+enough to run under a profiler.
+
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 2 --repeat 2
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 3 --seed 4 --png out.png
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scene 191 --view-width 1024
+
+Configurations: 1 the README tree at 1280x720, 2 the 512-sphere cheese at 3840x2160,
+3 a random tree at 1920x1080 (seeded), as in bench.py.
+"""
+from __future__ import annotations
+
+import argparse
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+sys.path.insert(0, str(HERE.parent))
+
+import numpy as np  # noqa: E402
+
+import csgrt  # noqa: E402
+from csgrt import scenes  # noqa: E402
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3])
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--repeat", type=int, default=2)
+    ap.add_argument("--exact", action="store_true", help="exact-box mode")
+    ap.add_argument("--batch-scenes", type=int, default=0, help="render the first N batch scenes x 4 views")
+    ap.add_argument("--batch-scene", type=int, default=-1, help="render one scene of the batched workload")
+    ap.add_argument("--view-width", type=int, default=0, help="with --batch-scene: its view of this size")
+    ap.add_argument("--png", default="", help="write the (single-view) frame as PNG")
+    ap.add_argument("--ppm", default="", help="write the (single-view) frame as PPM")
+    a = ap.parse_args(argv)
+
+    import torch
+    torch.cuda.set_device(0)
+    if a.batch_scenes > 0:
+        work = scenes.config_batch(a.seed, n_scenes=a.batch_scenes)
+        objs, views, outs = [], [], []
+        for text, vs in work:
+            sc = csgrt.Scene(text, exact_boxes=a.exact)
+            objs.append(sc)
+            for v in vs:
+                o = torch.empty(v.w * v.h, dtype=torch.int32, device="cuda")
+                outs.append(o)
+                views.append((sc, csgrt.Camera.from_floats(v.camera), v.light, v.w, v.h, {"rgba8": o.data_ptr()}))
+        b = csgrt.Batch(views)
+        for _ in range(a.repeat):
+            b.render()
+        torch.cuda.synchronize()
+        print("batch", b.info())
+        return 0
+
+    if a.batch_scene >= 0:
+        text = scenes.write_text(scenes.random_tree(a.seed * 100003 + a.batch_scene, 2, 2048, 12))
+        vs = scenes.config_views(4, a.seed * 100003 + a.batch_scene, 4)
+        view = next((v for v in vs if v.w == a.view_width), vs[0])
+    else:
+        text, view = scenes.config_scene_text(a.config, a.seed), scenes.config_views(a.config, a.seed)[0]
+    sc = csgrt.Scene(text, exact_boxes=a.exact)
+    cam = csgrt.Camera.from_floats(view.camera)
+    out = torch.empty(view.w * view.h, dtype=torch.int32, device="cuda")
+    for _ in range(a.repeat):
+        sc.render_ptrs(cam, view.light, view.w, view.h, rgba8=out.data_ptr())
+    torch.cuda.synchronize()
+    capped = sc.check()
+    print("view", view.w, view.h, sc.info(), "capped rays", capped)
+    frame = out.cpu().numpy().view(np.uint32)
+    if a.png:
+        csgrt.write_image(a.png, frame, view.w, view.h, "png")
+    if a.ppm:
+        csgrt.write_image(a.ppm, frame, view.w, view.h, "ppm")
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
