@@ -12,9 +12,9 @@
 // fill launches (so no host buffer has to outlive the call, and no copy from pageable
 // memory is involved).
 //
-// Work items are not listed: item i is block tile i - prefix[v] of the view v found by a
+// Work items are not listed: item i is warp tile i - prefix[v] of the view v found by a
 // binary search of the tile prefix, and the views are stored longest-first, so the launch
-// needs O(views) scratch rather than the O(tiles) work list of csg_batch.  The per-pixel
+// needs O(views) scratch, not a list of its tiles.  The per-pixel
 // code is pix::render_pixel, shared with the single-view and batched kernels, so every
 // view's planes are the bytes csg_render_planes writes.
 //
@@ -51,49 +51,50 @@ static_assert(kPrefixOffset + sizeof(int32_t) * (kMaxViews + 1) <= kScratchBytes
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
+// The persistent loop runs per warp: each warp takes its next 32-pixel warp tile from the
+// counter on its own, so no warp of a block waits for another (no block barrier in the
+// loop).  The item's view is the last one whose first item is not after it (binary
+// search of the prefix by lane 0).
 template <int SD, bool ROLLED>
 __global__ void __launch_bounds__(kThreads) render_views(const ViewsLaunch p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint16_t tab[27];
-    __shared__ int s_item, s_view;
     pix::load_table(tab);
     dev::SmemStacks<SD> st = pix::block_stacks<SD>(smem_raw);
     const pix::BlockSmem bs = pix::block_smem<SD>(smem_raw, p.live_words);
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int lane = threadIdx.x & 31;
     const int tw = 1 << p.tw_log2, th = 32 >> p.tw_log2;
-    const int ox = (warp & 1) * tw + (lane & (tw - 1));
-    const int oy = (warp >> 1) * th + (lane >> p.tw_log2);
+    const int ox = lane & (tw - 1), oy = lane >> p.tw_log2;
+    __syncthreads();  // the table is loaded
     while (true) {
-        __syncthreads();  // everyone has read s_item / s_view before they are overwritten
-        if (threadIdx.x == 0) {
-            const int it = atomicAdd(p.counter, 1);
-            int lo = 0, hi = p.n_views - 1;  // last view whose first item is <= it
+        int it = 0, vi = 0;
+        if (lane == 0) {
+            it = atomicAdd(p.counter, 1);
             if (it < p.n_items) {
+                int lo = 0, hi = p.n_views - 1;
                 while (lo < hi) {
                     const int mid = (lo + hi + 1) >> 1;
-                    if (p.prefix[mid] <= it) lo = mid;
+                    if (__ldg(&p.prefix[mid]) <= it) lo = mid;
                     else hi = mid - 1;
                 }
+                vi = lo;
             }
-            s_item = it;
-            s_view = lo;
         }
-        __syncthreads();
-        const int it = s_item;
+        it = __shfl_sync(0xffffffffu, it, 0);
+        vi = __shfl_sync(0xffffffffu, vi, 0);
         if (it >= p.n_items) break;
-        const int vi = s_view;
         const ViewRecord& v = p.views[vi];
-        const int tile = it - p.prefix[vi];
+        const int tile = it - __ldg(&p.prefix[vi]);
         const int tx = tile % v.tiles_x, ty = tile / v.tiles_x;
-        const int x = tx * 2 * tw + ox, y = ty * 2 * th + oy;
+        const int x = tx * tw + ox, y = ty * th + oy;
         const bool inside = x < v.view.w && y < v.view.h;
         pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab);
         if (p.remaining) {
-            if (v.host_out) __threadfence_system();  // this thread's host-mapped plane
+            if (v.host_out) __threadfence_system();  // this lane's host-mapped plane
             else __threadfence();
-            __syncthreads();
-            if (threadIdx.x == 0 && atomicSub(&p.remaining[vi], 1) == 1) {
+            __syncwarp();
+            if (lane == 0 && atomicSub(&p.remaining[vi], 1) == 1) {
                 __threadfence_system();
                 *reinterpret_cast<volatile unsigned int*>(&p.done_flags[vi]) = p.epoch;
             }
@@ -127,7 +128,7 @@ __global__ void fill_scratch(const __grid_constant__ FillChunk c, unsigned char*
 }
 
 template <int SD, bool ROLLED>
-cudaError_t launch_variant(const ViewsLaunch& l, int device, cudaStream_t stream)
+cudaError_t launch_variant(const ViewsLaunch& l, int device, cudaStream_t stream, int* grid_out)
 {
     const auto kernel = render_views<SD, ROLLED>;
     const size_t smem = pix::smem_bytes(SD, l.live_words);
@@ -136,8 +137,13 @@ cudaError_t launch_variant(const ViewsLaunch& l, int device, cudaStream_t stream
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
     if (e != cudaSuccess) return e;
+    // one block per resident slot, but no more warps than items
     int grid = sms * std::max(per_sm, 1);
-    grid = std::max(1, std::min(grid, l.n_items));
+    grid = std::max(1, std::min(grid, (l.n_items + kThreads / 32 - 1) / (kThreads / 32)));
+    if (grid_out) {
+        *grid_out = grid;
+        return cudaSuccess;
+    }
     kernel<<<grid, kThreads, smem, stream>>>(l);
     return cudaGetLastError();
 }
@@ -165,18 +171,40 @@ double view_cost(const csg_view& v)
 
 }  // namespace
 
-cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
+namespace {
+
+cudaError_t dispatch(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream,
+                     int* grid)
 {
     switch (stack_class) {
-        case 4: return rolled ? launch_variant<4, true>(l, device, stream) : launch_variant<4, false>(l, device, stream);
-        case 8: return rolled ? launch_variant<8, true>(l, device, stream) : launch_variant<8, false>(l, device, stream);
+        case 4:
+            return rolled ? launch_variant<4, true>(l, device, stream, grid)
+                          : launch_variant<4, false>(l, device, stream, grid);
+        case 8:
+            return rolled ? launch_variant<8, true>(l, device, stream, grid)
+                          : launch_variant<8, false>(l, device, stream, grid);
         case 12:
-            return rolled ? launch_variant<12, true>(l, device, stream) : launch_variant<12, false>(l, device, stream);
+            return rolled ? launch_variant<12, true>(l, device, stream, grid)
+                          : launch_variant<12, false>(l, device, stream, grid);
         case 16:
-            return rolled ? launch_variant<16, true>(l, device, stream) : launch_variant<16, false>(l, device, stream);
+            return rolled ? launch_variant<16, true>(l, device, stream, grid)
+                          : launch_variant<16, false>(l, device, stream, grid);
         default:
-            return rolled ? launch_variant<32, true>(l, device, stream) : launch_variant<32, false>(l, device, stream);
+            return rolled ? launch_variant<32, true>(l, device, stream, grid)
+                          : launch_variant<32, false>(l, device, stream, grid);
     }
+}
+
+}  // namespace
+
+cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
+{
+    return dispatch(l, stack_class, rolled, device, stream, nullptr);
+}
+
+cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, int device, int* grid)
+{
+    return dispatch(l, stack_class, rolled, device, nullptr, grid);
 }
 
 }  // namespace csgrt

@@ -1,5 +1,5 @@
-// Per-pixel body shared by the single-view kernel (render.cu) and the batched persistent
-// kernel (batch.cu): shared-memory layout of a 128-thread block, and one pixel's ray
+// Per-pixel body shared by the single-view kernel (render.cu) and the persistent
+// view-table kernel (noalloc.cu): shared-memory layout of a 128-thread block, and one pixel's ray
 // generation, liveness pre-pass, traversal, details, shading and output planes.
 #pragma once
 

@@ -16,7 +16,7 @@ namespace csgrt {
 struct ViewRecord {
     ViewParams view;
     unsigned long long* status;  // the scene's capped-ray counter
-    int32_t tiles_x;              // block tiles per row
+    int32_t tiles_x;              // warp tiles per row
     int32_t host_out;             // an output plane is host memory (system-scope fences)
 };
 static_assert(sizeof(ViewRecord) % 8 == 0, "view record alignment");
@@ -40,11 +40,11 @@ struct ViewsLaunch {
     unsigned int epoch;
 };
 
-// Block tiles of a w x h view for warp tile width tw (a block is 2x2 warp tiles).
+// Work items of a w x h view: warp tiles of tw x (32 / tw) pixels.
 inline int64_t view_tiles(int32_t w, int32_t h, int tw)
 {
     const int th = 32 / tw;
-    return (int64_t)((w + 2 * tw - 1) / (2 * tw)) * ((h + 2 * th - 1) / (2 * th));
+    return (int64_t)((w + tw - 1) / tw) * ((h + th - 1) / th);
 }
 
 inline int tile_log2(int tw)
@@ -65,12 +65,14 @@ inline void make_view_record(const DeviceScene& scene, unsigned long long* statu
     r.view.h = h;
     r.view.out = out;
     r.status = status;
-    r.tiles_x = (w + 2 * tw - 1) / (2 * tw);
+    r.tiles_x = (w + tw - 1) / tw;
     r.host_out = 0;
 }
 
 // Enqueues the view-table kernel variant for (stack_class, rolled) on `stream`, with a
-// grid that fills `device` once.
+// grid that fills `device` once (capturable: the host calls it makes enqueue nothing else).
 cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream);
+// The grid launch_views would use.
+cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, int device, int* grid);
 
 }  // namespace csgrt

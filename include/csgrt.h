@@ -149,7 +149,7 @@ typedef struct csg_batch csg_batch;
 
 typedef struct csg_batch_info {
     int32_t n_views;
-    int32_t n_items;      /* 128-pixel block tiles in the work list */
+    int32_t n_items;      /* work items: 32-pixel warp tiles */
     int32_t warp_tile_w;  /* warp tile width (height = 32 / width) */
     int32_t stack_class;  /* kernel variant: stack capacity ... */
     int32_t rolled;       /* ... and rolled GoTo loop */
@@ -157,7 +157,7 @@ typedef struct csg_batch_info {
     uint64_t device_bytes;
 } csg_batch_info;
 
-/* Builds the view descriptors and the longest-first work list on the current device.
+/* Builds the batch's view table (views most expensive first) on the current device.
  * The scenes and the output planes must stay valid while the batch is used. */
 int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out);
 int csg_batch_destroy(csg_batch* batch);
