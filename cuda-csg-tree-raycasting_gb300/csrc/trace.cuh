@@ -569,14 +569,16 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
         const int cl = __float_as_int(a0.w), cr = __float_as_int(a2.w);
         bool hl = false, hr = false;
         if (ROLLED) {
+            // both box tests side by side (independent work for the scheduler), the
+            // primitive tests in a rolled loop so that their code exists once
+            hl = active && box_hit(ray, a0, a1, 0.0f);
+            hr = active && box_hit(ray, a2, a3, 0.0f);
 #pragma unroll 1
             for (int j = 0; j < 2; ++j) {
-                const float4 lo = j ? a2 : a0, hi = j ? a3 : a1;
                 const int c = j ? cr : cl;
-                const bool h = active && box_hit(ray, lo, hi, 0.0f);
-                if (h && c < 0 && leaf_live_at_zero(ray, sc.geo, ~c, __float_as_int(hi.w))) lm.set_leaf(~c);
-                if (j) hr = h;
-                else hl = h;
+                const bool h = j ? hr : hl;
+                const int type = __float_as_int(j ? a3.w : a1.w);
+                if (h && c < 0 && leaf_live_at_zero(ray, sc.geo, ~c, type)) lm.set_leaf(~c);
             }
         } else {
             hl = active && box_hit(ray, a0, a1, 0.0f);
