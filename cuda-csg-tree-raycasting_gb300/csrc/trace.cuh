@@ -206,6 +206,32 @@ __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, floa
     return tmx > tmin;
 }
 
+// Conservative form of the box test at tmin = 0, for the liveness pre-pass: false only
+// when the reference's test culls the box for every tmin >= 0, i.e. when tmx <= 0 or
+// tmn > tmx; anything it cannot decide cheaply passes (the pre-pass only prunes, so a
+// pass is always safe).  From the reciprocal values t' (each with the sign of the
+// reference's t, infinities and NaNs where the reference has them, and otherwise within
+// 3u|t|): tmx' < 0 means some axis has both reference values <= 0, hence tmx <= 0; and
+// tmn' - tmx' > 2^-20 (|tmn'| + |tmx'|) with both magnitudes above 2^-100 means tmn > tmx.
+__device__ __forceinline__ bool box_may_pass_at_zero(const Ray& r, float4 lo, float4 hi)
+{
+    if (r.exact)
+        return box_hit_exact(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, 0.0f);
+    const float t1 = __fmul_rn(__fsub_rn(lo.x, r.o.x), r.inv.x);
+    const float t2 = __fmul_rn(__fsub_rn(hi.x, r.o.x), r.inv.x);
+    const float t3 = __fmul_rn(__fsub_rn(lo.y, r.o.y), r.inv.y);
+    const float t4 = __fmul_rn(__fsub_rn(hi.y, r.o.y), r.inv.y);
+    const float t5 = __fmul_rn(__fsub_rn(lo.z, r.o.z), r.inv.z);
+    const float t6 = __fmul_rn(__fsub_rn(hi.z, r.o.z), r.inv.z);
+    const float tmn = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
+    const float tmx = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
+    if (tmx < 0.0f) return false;
+    constexpr float kRel = 9.5367431640625e-07f;     // 2^-20
+    constexpr float kTiny = 7.888609052210118e-31f;  // 2^-100
+    const float an = fabsf(tmn), ax = fabsf(tmx);
+    return !(__fsub_rn(tmn, tmx) > kRel * __fadd_rn(an, ax) && fminf(an, ax) > kTiny);
+}
+
 // sphereHit (RaycastingKernels.cu:135-181)
 __device__ __forceinline__ void sphere_hit(const Ray& r, float4 g0, int32_t id, Hit& h, float tmin)
 {
@@ -544,8 +570,8 @@ __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* 
 
 // Liveness pre-pass: the warp walks the BVH over the leaves' own boxes together (its 32
 // rays are an 8x4 pixel tile, so they share most of the walk), each lane testing its own
-// ray, and every lane sets the bits of the leaves whose box passes at tmin = 0 and whose
-// primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
+// ray, and every lane sets the bits of the leaves whose box may pass at tmin = 0
+// (box_may_pass_at_zero) and whose primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
 // active == false only follow.  If the walk would overflow the warp's stack, every lane
 // falls back to an all-live mask (the traversal then decides everything itself).
 template <bool ROLLED>
@@ -571,8 +597,8 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
         if (ROLLED) {
             // both box tests side by side (independent work for the scheduler), the
             // primitive tests in a rolled loop so that their code exists once
-            hl = active && box_hit(ray, a0, a1, 0.0f);
-            hr = active && box_hit(ray, a2, a3, 0.0f);
+            hl = active && box_may_pass_at_zero(ray, a0, a1);
+            hr = active && box_may_pass_at_zero(ray, a2, a3);
 #pragma unroll 1
             for (int j = 0; j < 2; ++j) {
                 const int c = j ? cr : cl;
@@ -581,8 +607,8 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
                 if (h && c < 0 && leaf_live_at_zero(ray, sc.geo, ~c, type)) lm.set_leaf(~c);
             }
         } else {
-            hl = active && box_hit(ray, a0, a1, 0.0f);
-            hr = active && box_hit(ray, a2, a3, 0.0f);
+            hl = active && box_may_pass_at_zero(ray, a0, a1);
+            hr = active && box_may_pass_at_zero(ray, a2, a3);
             if (hl && cl < 0 && leaf_live_at_zero(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
             if (hr && cr < 0 && leaf_live_at_zero(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
         }
