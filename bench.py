@@ -35,8 +35,7 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "cuda-csg-tree-raycasting_gb300"))
 
-METRIC = json.loads((ROOT / "BASELINE.json").read_text())["metric"] if (ROOT / "BASELINE.json").exists() \
-    else "Mrays/s on 1 GB300"
+METRIC = "Mrays/s on 1 GB300, batched vs per-scene launch; p50/p99 request latency"
 PEAKS = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
 WORKLOADS = {
     1: "testWikipedia tree (9 nodes), 1280x720, camera (0,0,5) fov 60, light (-1,-1,-1)",

@@ -691,8 +691,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
 }
 
 // Per-ray traversal state of CSGRayCast (RaycastingKernels.cu:459-512), advanced one loop
-// iteration at a time by step() so that a lane can finish its ray and take another
-// while the rest of its warp is still traversing.
+// iteration at a time by tracer_step().
 struct Tracer {
     Ray ray;
     Hit L, R;

@@ -9,7 +9,7 @@ Reads the reference sources where they lie (default ``/root/reference``, overrid
   a ``bool`` function at RaycastingKernels.cu:335-336, which under optimisation makes
   every cylinder scene loop forever; ``hitPrimitive`` never reads the return value,
   RaycastingKernels.cu:113-133, so outputs are unchanged).  This copy never leaves the
-  machine (``.gpurunignore``).
+  machine it was made on (the repository's ignore lists exclude it).
 * ``oracle/_ref/libref_host.so`` -- the reference kernels, parser and camera compiled as
   host C++ with OpenMP (``oracle/ref_host_shim.cpp``).  Pins the C restatement.
 * ``oracle/_ref/ref_kernels.cubin`` -- the reference's ``RaycastKernel`` and
