@@ -1,8 +1,8 @@
 """CPU oracle for the CSG ray-casting path -- TEST INFRASTRUCTURE ONLY.
 
 Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
-may import this package, and only as the checker (or, for the baseline, as the timed
-CPU restatement of the reference).  The product never imports it.
+may import this package, and only to check results against it (or, for the baseline,
+as the timed CPU restatement of the reference).  The product never imports it.
 
 * :class:`Oracle` wraps ``oracle/_build/liboracle.so`` (``csg_oracle.c``), a plain-C
   restatement of the reference's parser, camera, traversal, intersections and shading.

@@ -2,7 +2,8 @@
  * parser, camera/light math, Kensler traversal, intersection tests and Phong shading.
  *
  * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and bench.py's
- * cpu_baseline leg use this library, as the checker; the product never links it.
+ * cpu_baseline leg use this library, to check results against it; the product never
+ * links it.
  *
  * Pinning: the "ieee" arithmetic mode is checked bit for bit against the reference's own
  * code compiled for the host (oracle/build_ref.py, oracle/ref_host_shim.cpp) on every
