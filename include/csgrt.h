@@ -149,25 +149,27 @@ typedef struct csg_batch csg_batch;
 
 typedef struct csg_batch_info {
     int32_t n_views;
-    int32_t n_items;      /* work items: 32-pixel warp tiles */
-    int32_t warp_tile_w;  /* warp tile width (height = 32 / width) */
-    int32_t stack_class;  /* kernel variant: stack capacity ... */
-    int32_t rolled;       /* ... and rolled GoTo loop */
-    int32_t grid;         /* persistent blocks */
+    int32_t n_items;      /* work items: 32-pixel warp tiles, all classes */
+    int32_t warp_tile_w;  /* warp tile width of the heaviest class (height = 32 / width) */
+    int32_t stack_class;  /* largest stack capacity of any class's kernel variant */
+    int32_t rolled;       /* some class uses the rolled GoTo loop */
+    int32_t grid;         /* persistent blocks of the largest class launch */
     uint64_t device_bytes;
 } csg_batch_info;
 
-/* Builds the batch's view table (views most expensive first) on the current device.
- * The scenes and the output planes must stay valid while the batch is used. */
+/* Builds the batch on the current device: views are grouped into tree-size classes (same
+ * kernel variant and live-mask size), each with its own view table (most expensive first)
+ * and persistent launch.  The scenes and the output planes must stay valid while the
+ * batch is used. */
 int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out);
 int csg_batch_destroy(csg_batch* batch);
-/* Renders every view in one persistent launch, replayed from a CUDA graph captured on the
- * first call (and again after a tile change); asynchronous on `stream`. */
+/* Renders every view: one CUDA graph, captured on the first call (and again after a tile
+ * change), whose branches are the classes' launches; asynchronous on `stream`. */
 int csg_batch_render(csg_batch* batch, void* stream);
-/* Sets the warp tile width (4, 8, 16 or 32 pixels; height 32 / width). */
+/* Sets the warp tile width of every class (4, 8, 16 or 32 pixels; height 32 / width). */
 int csg_batch_set_tile(csg_batch* batch, int32_t warp_tile_w);
-/* Autotuner: renders the batch with every warp tile shape, keeps the fastest, and reports
- * it and its time.  Synchronous. */
+/* Autotuner: times every warp tile shape for each class alone, keeps each class's fastest,
+ * and reports the heaviest class's shape and the whole batch's time.  Synchronous. */
 int csg_batch_tune(csg_batch* batch, void* stream, int32_t* best_tile_w, float* best_ms);
 int csg_batch_get_info(const csg_batch* batch, csg_batch_info* info);
 /* Synchronises `stream`; number of rays of the batch's renders stopped at the iteration
