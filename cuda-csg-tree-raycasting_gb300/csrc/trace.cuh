@@ -173,14 +173,17 @@ static __device__ __noinline__ bool box_hit_exact(float ox, float oy, float oz, 
 
 // The same decision from per-ray reciprocals, certified.  With s = b - o rounded as in
 // the reference, t' = rn(s * rn(1/d)) and t = rn(s / d) differ by at most 3u|t|
-// (u = 2^-24).  x -> x -+ 3u|x| are increasing maps and min/max commute with increasing
-// maps, so the reciprocal tmn' and tmx' are each within 3u of the reference's tmn and
-// tmx in the same relative sense.  The sign of tmx is therefore exact, and the two other
-// comparisons (tmn > tmx, tmx <= tmin) are exact whenever the operands differ by more
-// than 2^-20 of their magnitude (a 5x margin over the bound, covering the rounding of the
-// margin test itself).  Anything closer, and anything infinite, tiny or NaN, is decided
-// again with divisions; a ray with a subnormal direction component (whose reciprocal
-// overflows) always uses divisions (Ray::exact).
+// (u = 2^-24) in the normal range.  x -> x -+ 3u|x| are increasing maps and min/max
+// commute with increasing maps, so the reciprocal tmn' and tmx' are each within 3u of the
+// reference's tmn and tmx in the same relative sense.
+// The traversal's tmin is never negative (it starts at 0 and only moves to hit distances
+// beyond it), and then the reference's three culls (tmx < 0; tmn > tmx; tmn <= tmin and
+// tmx <= tmin) reduce to two: cull iff tmn > tmx or tmx <= tmin.  Each comparison is
+// decided from the reciprocal values when their difference exceeds 2^-20 of the
+// magnitudes involved plus 2^-120 (a 5x margin over the relative bound, and far above the
+// absolute error of subnormal results).  Infinite or NaN values make the margin test
+// fail, and a ray with a subnormal direction component (whose reciprocal overflows)
+// always uses divisions (Ray::exact); all of these are decided again with divisions.
 __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, float tmin)
 {
     if (r.exact)
@@ -193,17 +196,15 @@ __device__ __forceinline__ bool box_hit(const Ray& r, float4 lo, float4 hi, floa
     const float t6 = __fmul_rn(__fsub_rn(hi.z, r.o.z), r.inv.z);
     const float tmn = fmaxf(fmaxf(fminf(t1, t2), fminf(t3, t4)), fminf(t5, t6));
     const float tmx = fminf(fminf(fmaxf(t1, t2), fmaxf(t3, t4)), fmaxf(t5, t6));
-    const float an = fabsf(tmn), ax = fabsf(tmx);
     constexpr float kRel = 9.5367431640625e-07f;     // 2^-20
-    constexpr float kTiny = 7.888609052210118e-31f;  // 2^-100
-    const bool sure = (fabsf(__fsub_rn(tmn, tmx)) > kRel * (an + ax)) &&
-                      (fabsf(__fsub_rn(tmx, tmin)) > kRel * ax) && (an > kTiny) && (ax > kTiny) &&
-                      (ax < 3.0e38f) && (an < 3.0e38f);
+    constexpr float kAbs = 7.52316384526264e-37f;    // 2^-120
+    const float ax = fabsf(tmx);
+    const float d1 = __fsub_rn(tmn, tmx), d2 = __fsub_rn(tmx, tmin);
+    const bool sure = fabsf(d1) > __fmaf_rn(kRel, __fadd_rn(fabsf(tmn), ax), kAbs) &&
+                      fabsf(d2) > __fmaf_rn(kRel, ax, kAbs);
     if (!sure)
         return box_hit_exact(r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, lo.x, lo.y, lo.z, hi.x, hi.y, hi.z, tmin);
-    if (tmx < 0.0f) return false;
-    if (tmn > tmx) return false;
-    return tmx > tmin;
+    return d1 < 0.0f && d2 > 0.0f;
 }
 
 // Conservative form of the box test at tmin = 0, for the liveness pre-pass: false only
