@@ -51,10 +51,8 @@ WORKLOADS = {
 
 
 def dist_info():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from csgrt import replicas
+    return replicas.dist_info()
 
 
 class ClockSampler:
@@ -199,12 +197,10 @@ def run_engine(args):
     import torch
     import csgrt
 
+    from csgrt import replicas
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dist = replicas.init("nccl", torch.device("cuda", local))
     text, view = load_scene_and_view(args.config)
     w, h = view.w, view.h
     rays = w * h
@@ -228,8 +224,7 @@ def run_engine(args):
     t_start = torch.cuda.Event(enable_timing=True)
     t_end = torch.cuda.Event(enable_timing=True)
     with ClockSampler(local) as clk:
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
         torch.cuda.synchronize()
         t_start.record(stream)
         for i in range(args.steps):
@@ -239,17 +234,12 @@ def run_engine(args):
             ev[i][1].record(stream)
         t_end.record(stream)
         torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
     # The K steps' own device time: the CUDA events bracket each render; the L2 flush
     # between steps is outside them (its time is reported separately).
     bracket_ms = t_start.elapsed_time(t_end)
     launch_ms = [a.elapsed_time(b) for a, b in ev]
-    total_ms = float(np.sum(launch_ms))
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = replicas.max_over_ranks(dist, float(np.sum(launch_ms)), device="cuda")
 
     # end to end through the C ABI: render + copy of the frame to pinned host memory
     host = torch.empty(rays, dtype=torch.int32, pin_memory=True)
@@ -327,12 +317,10 @@ def run_batch(args):
     import csgrt
     from csgrt import scenes as S
 
+    from csgrt import replicas
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
-    dist = None
-    if ws > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dist = replicas.init("nccl", torch.device("cuda", local))
     work = S.config_batch(0)
     stream = torch.cuda.current_stream()
     scene_objs, views, outs = [], [], []
@@ -383,8 +371,7 @@ def run_batch(args):
         raise RuntimeError(f"{mismatched} batched views differ from their per-view renders")
 
     with ClockSampler(local) as clk:
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
         torch.cuda.synchronize()
         t0 = torch.cuda.Event(enable_timing=True)
         t1 = torch.cuda.Event(enable_timing=True)
@@ -392,14 +379,10 @@ def run_batch(args):
         b_ms = timed(batched, args.steps)
         t1.record(stream)
         torch.cuda.synchronize()
-        if dist:
-            dist.barrier()
+        replicas.barrier(dist)
     bracket_ms = t0.elapsed_time(t1)
-    total_ms = float(np.sum(b_ms))  # the steps' own events; the L2 flushes lie between them
-    if dist:
-        tt = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    # the steps' own events (the L2 flushes lie between them), slowest rank
+    total_ms = replicas.max_over_ranks(dist, float(np.sum(b_ms)), device="cuda")
     pv_steps = max(2, min(args.steps, 5))
     pv_ms = timed(per_view, pv_steps)
 
