@@ -304,15 +304,31 @@ def run_engine(args):
     if not args.no_cpu_baseline:
         res["cpu_baseline"] = cpu_baseline(text, view, seconds=args.cpu_seconds)
     scene.close()
+    if args.config == 2 and not args.no_extras:
+        # the metric's other two parts, on reduced runs: batched vs per-view launches
+        # (configuration 4) and request latency under load (configuration 5, 1,000 req/s)
+        sub = argparse.Namespace(**vars(args))
+        sub.steps, sub.warmup, sub.no_reference_cuda = 2, 3, True
+        b = run_batch(sub, sub=True)
+        res["batched"] = {"workload": WORKLOADS[4], "value": b["value"], "unit": "Mrays/s",
+                          "per_view_launches": b["per_view_launches"]["value"],
+                          "batched_vs_per_view": b["batched_vs_per_view"], "ms_per_batch": b["ms_per_step"],
+                          "steps": 2, "warmup": 3}
+        srv = run_serving(sub, sub=True, rates=(1000,), n_req=256)
+        row = srv["serving"][0]
+        res["serving"] = {"workload": WORKLOADS[5], "rate_rps": 1000, "requests": row["requests"],
+                          "batched": {k: row["batched"][k] for k in ("p50_ms", "p99_ms", "mrays_s")},
+                          "per_request": {k: row["per_request"][k] for k in ("p50_ms", "p99_ms", "mrays_s")}}
     print(json.dumps(res), flush=True)
     if dist:
         dist.destroy_process_group()
 
 
-def run_batch(args):
+def run_batch(args, sub=False):
     """Configuration 4: the 1024-view batch as one persistent graph-replayed launch
     (csg_batch_render, warp tile shape autotuned) against 1024 plain per-view launches
-    (csg_render_planes) of the same views on the same stream."""
+    (csg_render_planes) of the same views on the same stream.  With sub=True the result is
+    returned (for the default run's summary) instead of printed."""
     import torch
     import csgrt
     from csgrt import scenes as S
@@ -418,9 +434,9 @@ def run_batch(args):
     e2e_s = time.perf_counter() - t_e
 
     if rank != 0:
-        if dist:
+        if dist and not sub:
             dist.destroy_process_group()
-        return
+        return None
     value = ws * rays * args.steps / (total_ms * 1e-3) / 1e6
     pv_value = rays / (float(np.mean(pv_ms)) * 1e-3) / 1e6
     info = batch.info()
@@ -449,23 +465,27 @@ def run_batch(args):
                         "memory, wall clock; views and scenes resident"},
         "clocks": clk.summary(),
     }
-    print(json.dumps(res), flush=True)
     batch.close()
     for sc in scene_objs:
         sc.close()
+    if sub:
+        return res
+    print(json.dumps(res), flush=True)
     if dist:
         dist.destroy_process_group()
+    return res
 
 
 def _percentile(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
 
-def run_serving(args):
+def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
     """Configuration 5: the render server under open-loop Poisson arrivals, with continuous
     batching and with one single-view launch per request (the same server, requests
     flagged CSG_REQ_ALONE), at swept arrival rates.  Latency = completion - scheduled
-    arrival, measured inside the library on a steady clock."""
+    arrival, measured inside the library on a steady clock.  With sub=True the result is
+    returned instead of printed."""
     import torch
     import csgrt
     from csgrt import scenes as S
@@ -481,7 +501,6 @@ def run_serving(args):
         srv.preload(i)
     setup_s = time.perf_counter() - t_setup
     rng = np.random.default_rng(5)
-    n_req = 256
     sizes = [256, 512, 1024, 2048]
 
     def make_requests(n, alone, with_host=False):
@@ -505,7 +524,7 @@ def run_serving(args):
         for alone in (False, True):
             reqs, _, _ = make_requests(24, alone)
             srv.replay(reqs, np.zeros(len(reqs)))
-    rates = [100, 500, 1000, 2000, 5000]
+    rates = list(rates)
     sweep = []
     launches = 0
     with ClockSampler(local) as clk:
@@ -561,7 +580,10 @@ def run_serving(args):
         "server_stats": {k: st[k] for k in ("peak_bytes", "batches", "evictions", "rejected", "resident_scenes")},
         "clocks": clk.summary(),
     }
+    if sub:
+        return res_line
     print(json.dumps(res_line), flush=True)
+    return res_line
 
 
 def run_reference(args):
@@ -606,6 +628,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="default run: skip the reduced batched and serving measurements")
     ap.add_argument("--exact", action="store_true",
                     help="render with the optional exact-box mode (changes the output; for comparisons)")
     args = ap.parse_args()
