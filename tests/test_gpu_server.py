@@ -174,3 +174,50 @@ def test_server_replay_and_budget_evictions(csg):
         assert torch.equal(ref, hosts[i]), i
     for o in objs:
         o.close()
+
+
+@pytest.mark.gpu
+def test_server_release_while_batch_runs(csg):
+    """Requests retire one by one (per-view completion flags) and may be released while the
+    rest of their batch is still rendering; with several threads submitting, waiting and
+    releasing, every result is right when read and the server ends with no memory held."""
+    import torch
+    torch.cuda.set_device(0)
+    texts = _scene_texts()
+    objs = [csg.Scene(t) for t in texts]
+    reqs = _requests(csg, 120, len(texts), 33)
+    errors = []
+    with csg.Server(planes=1 | 4, keep_results=True, slots=2, max_batch_views=64) as srv:
+        for t in texts:
+            srv.add_scene(t)
+
+        def worker(k):
+            try:
+                for i in range(k, len(reqs), 4):
+                    sid, cam, light, w, h, _ = reqs[i]
+                    t = srv.submit(csg.Server.request(sid, cam, light, w, h))
+                    res = srv.wait(t, 60.0)
+                    assert res.status == csg.CSG_OK
+                    if i % 7 == 0:  # check some results before releasing them
+                        got = _dev(torch, res.planes.prim, w * h, "<i4").clone()
+                        ref = _alone(csg, torch, objs[sid], cam, light, w, h)["prim"]
+                        assert torch.equal(got, ref), i
+                    srv.release(t)
+            except Exception as e:  # noqa: BLE001 -- reported below
+                errors.append(repr(e))
+
+        th = [threading.Thread(target=worker, args=(k,)) for k in range(4)]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        assert not errors, errors
+        import time
+        deadline = time.time() + 30.0
+        while srv.stats()["output_bytes"] and time.time() < deadline:
+            time.sleep(0.01)  # launches whose requests were released early are still ending
+        st = srv.stats()
+        assert st["requests_done"] == len(reqs)
+        assert st["output_bytes"] == 0
+    for o in objs:
+        o.close()
