@@ -508,7 +508,13 @@ void pack_scene(const HostTree& t, PackedScene& out)
         k[1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
         k[2] = float4{r.minx, r.miny, r.minz, as_float(r.type)};
         k[3] = float4{r.maxx, r.maxy, r.maxz, as_float(r.prim)};
-        k[4] = float4{as_float(t.leaf_lo[nd.left]), as_float(t.leaf_hi[nd.left]), as_float(t.leaf_lo[nd.right]),
+        // Bit 30 of the left child's leaf_lo: test the right child first.  Operator
+        // children come before leaves and leaves go sphere, cube, cylinder, so that lanes of
+        // a warp at different nodes run the same kind of test together (the two tests are
+        // independent: disjoint leaf ranges, separate hit records).
+        auto prio = [](const RefNode& c) { return c.prim == -1 ? 0 : c.type == kSphere ? 1 : c.type == kCube ? 2 : 3; };
+        const int32_t swap = prio(r) < prio(l) ? (1 << 30) : 0;
+        k[4] = float4{as_float(t.leaf_lo[nd.left] | swap), as_float(t.leaf_hi[nd.left]), as_float(t.leaf_lo[nd.right]),
                       as_float(t.leaf_hi[nd.right])};
     }
     // live-mask granularity: one bit per 2^shift leaves, at most kLiveWordsMax words

@@ -58,7 +58,8 @@ void use_exact_boxes(HostTree& t);
 //                     child's type and primitive index in .w (as int bits), then the
 //                     children's leaf ranges:
 //                     {l.min.xyz, l.type} {l.max.xyz, l.prim} {r.min.xyz, r.type}
-//                     {r.max.xyz, r.prim} {l.leaf_lo, l.leaf_hi, r.leaf_lo, r.leaf_hi}
+//                     {r.max.xyz, r.prim} {l.leaf_lo, l.leaf_hi, r.leaf_lo, r.leaf_hi},
+//                     l.leaf_lo's bit 30 set when the right child is to be tested first
 //   geo[2p]    float4 {cx, cy, cz, p0} {p1, p2, p3, p4}
 //   color[p]   float4 {r, g, b, 0}
 //   bvh[4b]    a binary BVH over the leaves' own boxes (the reference's boxes), used

@@ -769,19 +769,26 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
         const bool op = T.ct.w <= kIntersection;
         bool gl = false, gr = false;
         if (ROLLED) {
+            // the two children in the order the scene compiler chose (operator children,
+            // then spheres, cubes, cylinders), so that a warp's lanes run one kind of test
+            // at a time
             const float4* kn = &kids[kKidsPerNode * T.cur];
             const int nj = op ? 2 : 1;
             const bool leaf_right = !op && (T.action & kGotoR);
+            int4 rg = make_int4(0, 0, 0, 0);
+            if (op) rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
+            const int first = (rg.x >> 30) & 1;
+            rg.x &= 0x3fffffff;
 #pragma unroll 1
-            for (int j = 0; j < nj; ++j) {
+            for (int k = 0; k < nj; ++k) {
+                const int j = k ^ first;
                 float4 lo, hi;
                 int rlo, rhi;
                 if (op) {
                     lo = __ldg(&kn[2 * j]);
                     hi = __ldg(&kn[2 * j + 1]);
-                    const int2 rg = __ldg(reinterpret_cast<const int2*>(&kn[4]) + j);
-                    rlo = rg.x;
-                    rhi = rg.y;
+                    rlo = j ? rg.z : rg.x;
+                    rhi = j ? rg.w : rg.y;
                 } else {
                     // GoTo landed on a leaf: one unboxed test into L or R
                     lo = make_float4(0.f, 0.f, 0.f, __int_as_float(T.ct.w));
@@ -806,7 +813,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
             const float4 k2 = __ldg(&kn[2]);
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
-            gl = child_test(T.ray, geo, k0, k1, rg.x, rg.y, T.L, T.tmin, lm);
+            gl = child_test(T.ray, geo, k0, k1, rg.x & 0x3fffffff, rg.y, T.L, T.tmin, lm);
             gr = child_test(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
         } else {
             Hit& H = (T.action & kGotoL) ? T.L : T.R;
