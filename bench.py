@@ -350,7 +350,9 @@ def run_batch(args, sub=False):
     rays = sum(v[3] * v[4] for v in views)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     batch = csgrt.Batch(views)
+    t_tune = time.perf_counter()
     tile_w, tune_ms = batch.tune(stream.cuda_stream)
+    tune_wall_s = time.perf_counter() - t_tune
 
     def per_view():
         for sc, cam, light, w, h, pl in views:
@@ -449,9 +451,15 @@ def run_batch(args, sub=False):
                    "l2": "flushed before every step by a 256 MiB device write, between the steps' events",
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "flush_ms_per_step": round((bracket_ms - total_ms) / args.steps, 4),
-        "batch": {"warp_tile": [tile_w, 32 // tile_w], "tune_ms": round(tune_ms, 3), "grid": info["grid"],
+        "batch": {"warp_tile": [tile_w, 32 // tile_w], "tuned_batch_ms": round(tune_ms, 3),
+                  "tune_wall_s": round(tune_wall_s, 1), "grid": info["grid"],
                   "items": info["n_items"], "stack_class": info["stack_class"], "rolled": info["rolled"],
-                  "kernel_ms": {"mean": float(np.mean(b_ms)), "min": float(np.min(b_ms))}},
+                  "kernel_ms": {"mean": float(np.mean(b_ms)), "min": float(np.min(b_ms))},
+                  "classes": [{"views": c["n_views"], "stack": c["stack_class"], "rolled": c["rolled"],
+                               "live_words": c["live_words"], "warp_tile": [c["warp_tile_w"], 32 // c["warp_tile_w"]],
+                               "warps_per_block": c["warps_per_block"],
+                               "stacks": "local" if c["local_stacks"] else "shared",
+                               "tuned_ms": round(c["tuned_ms"], 3)} for c in batch.classes()]},
         "per_view_launches": {"value": round(pv_value, 3), "unit": "Mrays/s", "launches": len(views),
                               "ms_per_step": round(float(np.mean(pv_ms)), 3),
                               "note": "the same 1024 views, one csg_render_planes launch each, one stream"},

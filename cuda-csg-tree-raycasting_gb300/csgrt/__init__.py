@@ -41,7 +41,7 @@ EXPORTED = [
     "csg_batch_get_info", "csg_batch_check", "csg_render_views_noalloc",
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
-    "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex",
+    "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex", "csg_batch_set_shape", "csg_batch_get_class",
 ]
 
 _vp = ctypes.c_void_p
@@ -77,7 +77,14 @@ class csg_view(ctypes.Structure):
 
 class csg_batch_info(ctypes.Structure):
     _fields_ = [("n_views", _i32), ("n_items", _i32), ("warp_tile_w", _i32), ("stack_class", _i32),
-                ("rolled", _i32), ("grid", _i32), ("device_bytes", ctypes.c_uint64)]
+                ("rolled", _i32), ("grid", _i32), ("device_bytes", ctypes.c_uint64), ("n_classes", _i32),
+                ("warps_per_block", _i32), ("local_stacks", _i32)]
+
+
+class csg_batch_class_info(ctypes.Structure):
+    _fields_ = [("n_views", _i32), ("stack_class", _i32), ("rolled", _i32), ("live_words", _i32),
+                ("warp_tile_w", _i32), ("warps_per_block", _i32), ("local_stacks", _i32), ("grid", _i32),
+                ("n_items", _i32), ("tuned_ms", _f)]
 
 
 CSG_PLANE_RGBA8, CSG_PLANE_T, CSG_PLANE_PRIM, CSG_PLANE_NORMAL, CSG_PLANE_RGBA32F = 1, 2, 4, 8, 16
@@ -158,6 +165,8 @@ def lib() -> ctypes.CDLL:
     L.csg_batch_set_tile.argtypes = [_vp, _i32]
     L.csg_batch_tune.argtypes = [_vp, _vp, ctypes.POINTER(_i32), ctypes.POINTER(_f)]
     L.csg_batch_get_info.argtypes = [_vp, ctypes.POINTER(csg_batch_info)]
+    L.csg_batch_set_shape.argtypes = [_vp, _i32, _i32]
+    L.csg_batch_get_class.argtypes = [_vp, _i32, ctypes.POINTER(csg_batch_class_info)]
     L.csg_batch_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_render_views_noalloc.argtypes = [ctypes.POINTER(csg_view), _i32, _i32, _vp]
     L.csg_server_create.argtypes = [ctypes.POINTER(csg_server_config), ctypes.POINTER(_vp)]
@@ -412,6 +421,19 @@ class Batch:
 
     def set_tile(self, warp_tile_w: int):
         check(lib().csg_batch_set_tile(self.h, warp_tile_w))
+
+    def set_shape(self, warps_per_block: int = 4, local_stacks: bool = False):
+        """Block shape of every class's launch: (4, False), (4, True), (2, False) or (8, False)."""
+        check(lib().csg_batch_set_shape(self.h, warps_per_block, int(bool(local_stacks))))
+
+    def classes(self) -> list:
+        """Per tree-size class (heaviest first): its kernel variant and configuration."""
+        out = []
+        for k in range(self.info()["n_classes"]):
+            c = csg_batch_class_info()
+            check(lib().csg_batch_get_class(self.h, k, ctypes.byref(c)))
+            out.append({n: getattr(c, n) for n, _ in csg_batch_class_info._fields_})
+        return out
 
     def tune(self, stream=0):
         tw, ms = _i32(), _f()

@@ -4,8 +4,8 @@
 // variant (stack capacity, rolled or unrolled GoTo) and a similar live-mask size (the
 // shared memory per block, hence the blocks per SM) form one class.  Each class has its
 // own view table (views most expensive first), its own persistent view-table launch
-// (views.hpp) with that class's variant, and its own warp tile shape, chosen by the
-// autotuner per class.  All class launches are captured into one CUDA graph as
+// (views.hpp) with that class's variant, and its own warp tile shape and block shape
+// (warps per block, stack placement), chosen by the autotuner per class.  All class launches are captured into one CUDA graph as
 // independent branches, so they share the GPU: the light classes fill the SMs the heavy
 // class's tail leaves idle.
 #include <algorithm>
@@ -33,6 +33,8 @@ struct BatchClass {
     int* d_counter = nullptr;
     csgrt::ViewsLaunch launch{};
     int tile_w = 8;
+    csgrt::ViewsShape shape{};
+    float tuned_ms = 0.f;  // this class alone at its chosen configuration (after tuning)
     int grid = 0;
     cudaStream_t stream = nullptr;  // its branch of the captured graph
     cudaEvent_t done = nullptr;
@@ -97,7 +99,18 @@ int build_table(csg_batch* b, BatchClass& c, int tw)
     c.launch.tw_log2 = csgrt::tile_log2(tw);
     c.tile_w = tw;
     drop_graph(b);
-    if (csgrt::views_grid(c.launch, c.stack_class, c.rolled, b->device, &c.grid) != cudaSuccess) return CSG_E_CUDA;
+    if (csgrt::views_grid(c.launch, c.stack_class, c.rolled, c.shape, b->device, &c.grid) != cudaSuccess)
+        return CSG_E_CUDA;
+    return CSG_OK;
+}
+
+// Class c's block shape (warps per block, stack placement).
+int set_shape(csg_batch* b, BatchClass& c, csgrt::ViewsShape s)
+{
+    c.shape = s;
+    drop_graph(b);
+    if (csgrt::views_grid(c.launch, c.stack_class, c.rolled, c.shape, b->device, &c.grid) != cudaSuccess)
+        return CSG_E_CUDA;
     return CSG_OK;
 }
 
@@ -105,7 +118,7 @@ int build_table(csg_batch* b, BatchClass& c, int tw)
 cudaError_t enqueue_class(const csg_batch* b, const BatchClass& c, cudaStream_t st)
 {
     cudaError_t e = cudaMemsetAsync(c.d_counter, 0, sizeof(int), st);
-    if (e == cudaSuccess) e = csgrt::launch_views(c.launch, c.stack_class, c.rolled, b->device, st);
+    if (e == cudaSuccess) e = csgrt::launch_views(c.launch, c.stack_class, c.rolled, c.shape, b->device, st);
     return e;
 }
 
@@ -284,8 +297,10 @@ int csg_batch_render(csg_batch* b, void* stream)
     return cudaGraphLaunch(b->graph, static_cast<cudaStream_t>(stream)) == cudaSuccess ? CSG_OK : CSG_E_CUDA;
 }
 
-// Autotuner: for each class alone, every warp tile shape (three timed launches each);
-// keeps each class's fastest, then times the whole batch.
+// Autotuner, per class alone (one warm-up and three timed launches per configuration):
+// every warp tile shape with the default block shape, then every other block shape
+// (warps per block, stack placement) with the best tile; keeps each class's fastest,
+// then times the whole batch.
 int csg_batch_tune(csg_batch* b, void* stream, int32_t* best_tile_w, float* best_ms)
 {
     if (!b) return CSG_E_ARG;
@@ -296,6 +311,7 @@ int csg_batch_tune(csg_batch* b, void* stream, int32_t* best_tile_w, float* best
     for (BatchClass& c : b->classes) {
         int best = 8;
         float best_t = 0.f;
+        if ((rc = set_shape(b, c, csgrt::kViewsShapes[0])) != CSG_OK) break;
         for (int tw : kTileShapes) {
             float ms = 0.f;
             if ((rc = build_table(b, c, tw)) != CSG_OK) break;
@@ -307,6 +323,19 @@ int csg_batch_tune(csg_batch* b, void* stream, int32_t* best_tile_w, float* best
         }
         if (rc != CSG_OK) break;
         if ((rc = build_table(b, c, best)) != CSG_OK) break;
+        csgrt::ViewsShape best_shape = csgrt::kViewsShapes[0];
+        for (int k = 1; k < 4 && rc == CSG_OK; ++k) {
+            float ms = 0.f;
+            if ((rc = set_shape(b, c, csgrt::kViewsShapes[k])) != CSG_OK) break;
+            if ((rc = time_class(b, c, st, e0, e1, 3, &ms)) != CSG_OK) break;
+            if (ms < best_t) {
+                best_t = ms;
+                best_shape = csgrt::kViewsShapes[k];
+            }
+        }
+        if (rc != CSG_OK) break;
+        if ((rc = set_shape(b, c, best_shape)) != CSG_OK) break;
+        c.tuned_ms = best_t;
     }
     float whole = 0.f;
     if (rc == CSG_OK) rc = csg_batch_render(b, stream);  // capture and warm-up
@@ -322,6 +351,35 @@ int csg_batch_tune(csg_batch* b, void* stream, int32_t* best_tile_w, float* best
     if (rc != CSG_OK) return rc;
     if (best_tile_w) *best_tile_w = b->classes.empty() ? 8 : b->classes.front().tile_w;
     if (best_ms) *best_ms = whole;
+    return CSG_OK;
+}
+
+int csg_batch_set_shape(csg_batch* b, int32_t warps_per_block, int32_t local_stacks)
+{
+    if (!b) return CSG_E_ARG;
+    const csgrt::ViewsShape s{warps_per_block, local_stacks != 0};
+    if ((local_stacks != 0 && local_stacks != 1) || !csgrt::valid_shape(s)) return CSG_E_ARG;
+    for (BatchClass& c : b->classes) {
+        const int rc = set_shape(b, c, s);
+        if (rc != CSG_OK) return rc;
+    }
+    return CSG_OK;
+}
+
+int csg_batch_get_class(const csg_batch* b, int32_t k, csg_batch_class_info* info)
+{
+    if (!b || !info || k < 0 || k >= (int32_t)b->classes.size()) return CSG_E_ARG;
+    const BatchClass& c = b->classes[k];
+    info->n_views = (int32_t)c.views.size();
+    info->stack_class = c.stack_class;
+    info->rolled = c.rolled ? 1 : 0;
+    info->live_words = c.live_words;
+    info->warp_tile_w = c.tile_w;
+    info->warps_per_block = c.shape.warps;
+    info->local_stacks = c.shape.local_stacks ? 1 : 0;
+    info->grid = c.grid;
+    info->n_items = c.launch.n_items;
+    info->tuned_ms = c.tuned_ms;
     return CSG_OK;
 }
 
@@ -343,6 +401,9 @@ int csg_batch_get_info(const csg_batch* b, csg_batch_info* info)
     info->rolled = rolled;
     info->grid = grid;
     info->device_bytes = b->bytes;
+    info->n_classes = (int32_t)b->classes.size();
+    info->warps_per_block = b->classes.empty() ? 4 : b->classes.front().shape.warps;
+    info->local_stacks = (!b->classes.empty() && b->classes.front().shape.local_stacks) ? 1 : 0;
     return CSG_OK;
 }
 

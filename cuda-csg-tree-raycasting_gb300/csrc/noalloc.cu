@@ -34,12 +34,10 @@
 #include "csgrt.h"
 #include "pixel.cuh"
 #include "scene_handle.hpp"
-#include "views.hpp"
+#include "views_kernel.cuh"
 
 namespace csgrt {
 namespace {
-
-using pix::kThreads;
 
 constexpr int kMaxViews = CSG_NOALLOC_MAX_VIEWS;
 
@@ -50,62 +48,6 @@ constexpr size_t kScratchBytes = 1u << 20;
 static_assert(kPrefixOffset + sizeof(int32_t) * (kMaxViews + 1) <= kScratchBytes, "scratch too small");
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
-
-// The persistent loop runs per warp: each warp takes its next 32-pixel warp tile from the
-// counter on its own, so no warp of a block waits for another (no block barrier in the
-// loop).  The item's view is the last one whose first item is not after it (binary
-// search of the prefix by lane 0).
-// Minimum resident blocks per SM asked of the register allocator (a tuning knob): six
-// blocks (80 registers) ran the 1,024-view batch 8% faster than five (96 registers).
-#ifndef CSG_VIEWS_MIN_BLOCKS
-#define CSG_VIEWS_MIN_BLOCKS 6
-#endif
-template <int SD, bool ROLLED>
-__global__ void __launch_bounds__(kThreads, CSG_VIEWS_MIN_BLOCKS) render_views(const ViewsLaunch p)
-{
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ uint16_t tab[27];
-    pix::load_table(tab);
-    dev::SmemStacks<SD> st = pix::block_stacks<SD>(smem_raw);
-    const pix::BlockSmem bs = pix::block_smem<SD>(smem_raw, p.live_words);
-    const int lane = threadIdx.x & 31;
-    const int tw = 1 << p.tw_log2, th = 32 >> p.tw_log2;
-    const int ox = lane & (tw - 1), oy = lane >> p.tw_log2;
-    __syncthreads();  // the table is loaded
-    while (true) {
-        int it = 0, vi = 0;
-        if (lane == 0) {
-            it = atomicAdd(p.counter, 1);
-            if (it < p.n_items) {
-                int lo = 0, hi = p.n_views - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) >> 1;
-                    if (__ldg(&p.prefix[mid]) <= it) lo = mid;
-                    else hi = mid - 1;
-                }
-                vi = lo;
-            }
-        }
-        it = __shfl_sync(0xffffffffu, it, 0);
-        vi = __shfl_sync(0xffffffffu, vi, 0);
-        if (it >= p.n_items) break;
-        const ViewRecord& v = p.views[vi];
-        const int tile = it - __ldg(&p.prefix[vi]);
-        const int tx = tile % v.tiles_x, ty = tile / v.tiles_x;
-        const int x = tx * tw + ox, y = ty * th + oy;
-        const bool inside = x < v.view.w && y < v.view.h;
-        pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab);
-        if (p.remaining) {
-            if (v.host_out) __threadfence_system();  // this lane's host-mapped plane
-            else __threadfence();
-            __syncwarp();
-            if (lane == 0 && atomicSub(&p.remaining[vi], 1) == 1) {
-                __threadfence_system();
-                *reinterpret_cast<volatile unsigned int*>(&p.done_flags[vi]) = p.epoch;
-            }
-        }
-    }
-}
 
 // One fill launch: up to kChunk view records and their tile prefixes, passed by value.
 constexpr int kChunk = 112;
@@ -132,27 +74,6 @@ __global__ void fill_scratch(const __grid_constant__ FillChunk c, unsigned char*
     }
 }
 
-template <int SD, bool ROLLED>
-cudaError_t launch_variant(const ViewsLaunch& l, int device, cudaStream_t stream, int* grid_out)
-{
-    const auto kernel = render_views<SD, ROLLED>;
-    const size_t smem = pix::smem_bytes(SD, l.live_words);
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int sms = 0, per_sm = 0;
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kThreads, smem);
-    if (e != cudaSuccess) return e;
-    // one block per resident slot, but no more warps than items
-    int grid = sms * std::max(per_sm, 1);
-    grid = std::max(1, std::min(grid, (l.n_items + kThreads / 32 - 1) / (kThreads / 32)));
-    if (grid_out) {
-        *grid_out = grid;
-        return cudaSuccess;
-    }
-    kernel<<<grid, kThreads, smem, stream>>>(l);
-    return cudaGetLastError();
-}
-
 // Address of the scratch array on each device, looked up on the first call there.
 constexpr int kMaxDevices = 64;
 std::atomic<unsigned char*> g_scratch_addr[kMaxDevices];
@@ -176,41 +97,29 @@ double view_cost(const csg_view& v)
 
 }  // namespace
 
-namespace {
+// The other shapes are instantiated in views_shapes_*.cu (compiled in parallel).
+extern template cudaError_t launch_views_shape<64, false>(const ViewsLaunch&, int, bool, int, cudaStream_t, int*);
+extern template cudaError_t launch_views_shape<256, false>(const ViewsLaunch&, int, bool, int, cudaStream_t, int*);
+extern template cudaError_t launch_views_shape<128, true>(const ViewsLaunch&, int, bool, int, cudaStream_t, int*);
 
-cudaError_t dispatch(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream,
-                     int* grid)
+cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, ViewsShape shape, int device,
+                         cudaStream_t stream)
 {
-    switch (stack_class) {
-        case 4:
-            return rolled ? launch_variant<4, true>(l, device, stream, grid)
-                          : launch_variant<4, false>(l, device, stream, grid);
-        case 8:
-            return rolled ? launch_variant<8, true>(l, device, stream, grid)
-                          : launch_variant<8, false>(l, device, stream, grid);
-        case 12:
-            return rolled ? launch_variant<12, true>(l, device, stream, grid)
-                          : launch_variant<12, false>(l, device, stream, grid);
-        case 16:
-            return rolled ? launch_variant<16, true>(l, device, stream, grid)
-                          : launch_variant<16, false>(l, device, stream, grid);
-        default:
-            return rolled ? launch_variant<32, true>(l, device, stream, grid)
-                          : launch_variant<32, false>(l, device, stream, grid);
-    }
+    if (shape.local_stacks) return launch_views_shape<128, true>(l, stack_class, rolled, device, stream, nullptr);
+    if (shape.warps == 2) return launch_views_shape<64, false>(l, stack_class, rolled, device, stream, nullptr);
+    if (shape.warps == 8) return launch_views_shape<256, false>(l, stack_class, rolled, device, stream, nullptr);
+    return launch_views_shape<128, false>(l, stack_class, rolled, device, stream, nullptr);
 }
 
-}  // namespace
-
-cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream)
+cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, ViewsShape shape, int device, int* grid)
 {
-    return dispatch(l, stack_class, rolled, device, stream, nullptr);
+    if (shape.local_stacks) return launch_views_shape<128, true>(l, stack_class, rolled, device, nullptr, grid);
+    if (shape.warps == 2) return launch_views_shape<64, false>(l, stack_class, rolled, device, nullptr, grid);
+    if (shape.warps == 8) return launch_views_shape<256, false>(l, stack_class, rolled, device, nullptr, grid);
+    return launch_views_shape<128, false>(l, stack_class, rolled, device, nullptr, grid);
 }
 
-cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, int device, int* grid)
-{
-    return dispatch(l, stack_class, rolled, device, nullptr, grid);
-}
+template cudaError_t launch_views_shape<128, false>(const ViewsLaunch&, int, bool, int, cudaStream_t, int*);
 
 }  // namespace csgrt
 
@@ -287,5 +196,6 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
     l.remaining = nullptr;
     l.done_flags = nullptr;
     l.epoch = 0;
-    return launch_views(l, stack_class_for_depth(sd), rolled, device, st) == cudaSuccess ? CSG_OK : CSG_E_CUDA;
+    return launch_views(l, stack_class_for_depth(sd), rolled, ViewsShape{}, device, st) == cudaSuccess ? CSG_OK
+                                                                                                  : CSG_E_CUDA;
 }

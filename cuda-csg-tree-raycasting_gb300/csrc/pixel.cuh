@@ -1,6 +1,6 @@
 // Per-pixel body shared by the single-view kernel (render.cu) and the persistent
-// view-table kernel (noalloc.cu): shared-memory layout of a 128-thread block, and one pixel's ray
-// generation, liveness pre-pass, traversal, details, shading and output planes.
+// view-table kernel (views_kernel.cuh): shared-memory layout of a block, and one pixel's
+// ray generation, liveness pre-pass, traversal, details, shading and output planes.
 #pragma once
 
 #include "render.hpp"
@@ -9,47 +9,51 @@
 namespace csgrt {
 namespace pix {
 
-constexpr int kThreads = 128;  // 4 warps per block
+constexpr int kThreads = 128;  // 4 warps per block: the single-view kernel, the default view-table shape
 
-// Shared memory of a block: the per-ray primitive and time stacks (SD slots), the per-ray
-// live masks (live_words words) and one BVH stack per warp.
-template <int SD>
-__host__ __device__ constexpr size_t stack_bytes()
+// Shared memory of an nt-thread block: the per-ray primitive and time stacks (SD slots;
+// none when the stacks are in local memory), the per-ray live masks (live_words words)
+// and one BVH stack per warp.
+inline size_t smem_bytes(int sd, int live_words, int nt = kThreads, bool local_stacks = false)
 {
-    return (size_t)SD * kThreads * 12;
-}
-inline size_t smem_bytes(int sd, int live_words)
-{
-    return (size_t)sd * kThreads * 12 + (size_t)live_words * kThreads * 4 +
-           (size_t)(kThreads / 32) * dev::kWarpStack * 4;
+    return (local_stacks ? 0 : (size_t)sd * nt * 12) + (size_t)live_words * nt * 4 +
+           (size_t)(nt / 32) * dev::kWarpStack * 4;
 }
 
 struct BlockSmem {
     int* wstack;    // this warp's BVH stack
-    uint32_t* live; // live-mask base (word k of thread t at live[k * kThreads + t])
+    uint32_t* live; // live-mask base (word k of thread t at live[k * nt + t])
+    int nt;         // threads per block
 };
 
-template <int SD>
+template <int SD, int NT>
 __device__ __forceinline__ dev::SmemStacks<SD> block_stacks(unsigned char* smem_raw)
 {
     dev::SmemStacks<SD> st;
-    st.nt = kThreads;
+    st.nt = NT;
     st.tid = threadIdx.x;
     st.pt = reinterpret_cast<float*>(smem_raw);
-    st.pb = reinterpret_cast<uint32_t*>(st.pt + SD * kThreads);
-    st.tt = reinterpret_cast<float*>(st.pb + SD * kThreads);
+    st.pb = reinterpret_cast<uint32_t*>(st.pt + SD * NT);
+    st.tt = reinterpret_cast<float*>(st.pb + SD * NT);
     st.np = 0;
     st.ntm = 0;
     return st;
 }
 
 template <int SD>
+__device__ __forceinline__ void init_stacks(dev::LocalStacks<SD>& st)
+{
+    st.np = 0;
+    st.ntm = 0;
+}
+
+template <int SD, int NT, bool LOCAL>
 __device__ __forceinline__ BlockSmem block_smem(unsigned char* smem_raw, int live_words_alloc)
 {
     BlockSmem b;
-    b.live = reinterpret_cast<uint32_t*>(smem_raw + stack_bytes<SD>());
-    b.wstack = reinterpret_cast<int*>(b.live + (size_t)live_words_alloc * kThreads) +
-               (threadIdx.x >> 5) * dev::kWarpStack;
+    b.live = reinterpret_cast<uint32_t*>(smem_raw + (LOCAL ? 0 : (size_t)SD * NT * 12));
+    b.wstack = reinterpret_cast<int*>(b.live + (size_t)live_words_alloc * NT) + (threadIdx.x >> 5) * dev::kWarpStack;
+    b.nt = NT;
     return b;
 }
 
@@ -87,14 +91,14 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
 
 // One pixel.  Must be called by all 32 lanes of a warp (the pre-pass walks the BVH
 // warp-cooperatively); lanes with inside == false only follow the walk.
-template <int SD, bool ROLLED>
+template <int SD, bool ROLLED, class Stacks>
 __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long long* status, uint32_t iter_cap,
-                                             int x, int y, bool inside, dev::SmemStacks<SD>& st,
-                                             const BlockSmem& bs, const uint16_t* tab)
+                                             int x, int y, bool inside, Stacks& st, const BlockSmem& bs,
+                                             const uint16_t* tab)
 {
     dev::LiveMask lm;
     lm.w = bs.live + threadIdx.x;
-    lm.nt = kThreads;
+    lm.nt = bs.nt;
     lm.shift = p.scene.live_shift;
     lm.words = p.scene.live_words;
     lm.sum = 0;

@@ -31,6 +31,13 @@ struct RenderParams {
 #ifndef CSG_UNROLLED_MIN_BLOCKS
 #define CSG_UNROLLED_MIN_BLOCKS 6
 #endif
+// Placement of the per-ray primitive and time stacks (a tuning knob): 1 = per-thread
+// local memory, 0 = block shared memory.
+#ifndef CSG_TILED_LOCAL_STACKS
+#define CSG_TILED_LOCAL_STACKS 0
+#endif
+constexpr bool kLocalStacks = CSG_TILED_LOCAL_STACKS != 0;
+
 template <int SD, bool ROLLED>
 __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG_UNROLLED_MIN_BLOCKS)
     render_tiled(const RenderParams p)
@@ -38,8 +45,10 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint16_t tab[27];
     pix::load_table(tab);
-    dev::SmemStacks<SD> st = pix::block_stacks<SD>(smem_raw);
-    const pix::BlockSmem bs = pix::block_smem<SD>(smem_raw, p.view.scene.live_words);
+    typename std::conditional<kLocalStacks, dev::LocalStacks<SD>, dev::SmemStacks<SD>>::type st;
+    if constexpr (kLocalStacks) pix::init_stacks(st);
+    else st = pix::block_stacks<SD, kThreads>(smem_raw);
+    const pix::BlockSmem bs = pix::block_smem<SD, kThreads, kLocalStacks>(smem_raw, p.view.scene.live_words);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
     const int y = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
@@ -50,14 +59,15 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
 template <int SD, bool ROLLED>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
-    const size_t smem = pix::smem_bytes(SD, p.view.scene.live_words);
+    const size_t smem = pix::smem_bytes(SD, p.view.scene.live_words, kThreads, kLocalStacks);
     // Above the default 48 KiB per block the kernel needs the opt-in; set it once for the
     // largest layout any scene can ask for (kLiveWordsMax live words).
     static bool attr_set = false;
     if (!attr_set) {
         const cudaError_t e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)pix::smem_bytes(SD, kLiveWordsMax));
+                                                   (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads,
+                                                                        kLocalStacks));
         if (e != cudaSuccess) return e;
         attr_set = true;
     }

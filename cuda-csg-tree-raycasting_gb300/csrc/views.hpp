@@ -69,10 +69,35 @@ inline void make_view_record(const DeviceScene& scene, unsigned long long* statu
     r.host_out = 0;
 }
 
-// Enqueues the view-table kernel variant for (stack_class, rolled) on `stream`, with a
-// grid that fills `device` once (capturable: the host calls it makes enqueue nothing else).
-cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream);
+// Block shape of a view-table launch: warps per block (2, 4 or 8) and where the per-ray
+// primitive and time stacks live (block shared memory, or per-thread local memory, which
+// leaves shared memory to the live masks and more of the SM's L1 to the scene).  Every
+// shape renders the same bytes; the batch autotuner picks one per tree-size class.
+struct ViewsShape {
+    int warps = 4;
+    bool local_stacks = false;
+};
+constexpr ViewsShape kViewsShapes[4] = {{4, false}, {2, false}, {8, false}, {4, true}};
+
+inline bool valid_shape(const ViewsShape& s)
+{
+    for (const ViewsShape& k : kViewsShapes)
+        if (k.warps == s.warps && k.local_stacks == s.local_stacks) return true;
+    return false;
+}
+
+// Enqueues the view-table kernel variant for (stack_class, rolled, shape) on `stream`,
+// with a grid that fills `device` once (capturable: the host calls it makes enqueue
+// nothing else).
+cudaError_t launch_views(const ViewsLaunch& l, int stack_class, bool rolled, ViewsShape shape, int device,
+                         cudaStream_t stream);
 // The grid launch_views would use.
-cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, int device, int* grid);
+cudaError_t views_grid(const ViewsLaunch& l, int stack_class, bool rolled, ViewsShape shape, int device, int* grid);
+
+// One block shape's launcher (views_kernel.cuh), instantiated for the shapes of
+// kViewsShapes; grid_out != null only computes the grid.
+template <int NT, bool LOCAL>
+cudaError_t launch_views_shape(const ViewsLaunch& l, int stack_class, bool rolled, int device, cudaStream_t stream,
+                               int* grid_out);
 
 }  // namespace csgrt

@@ -155,7 +155,25 @@ typedef struct csg_batch_info {
     int32_t rolled;       /* some class uses the rolled GoTo loop */
     int32_t grid;         /* persistent blocks of the largest class launch */
     uint64_t device_bytes;
+    int32_t n_classes;        /* tree-size classes (one persistent launch each) */
+    int32_t warps_per_block;  /* block shape of the heaviest class: warps per block */
+    int32_t local_stacks;     /* ... and its per-ray stacks in local (1) or shared (0) memory */
 } csg_batch_info;
+
+/* One tree-size class of a batch: its kernel variant and the configuration the autotuner
+ * (or csg_batch_set_tile / csg_batch_set_shape) gave it. */
+typedef struct csg_batch_class_info {
+    int32_t n_views;
+    int32_t stack_class;      /* per-ray stack capacity of the kernel variant */
+    int32_t rolled;           /* rolled GoTo loop */
+    int32_t live_words;       /* live-mask words per ray (a power of two) */
+    int32_t warp_tile_w;      /* warp tile width (height 32 / width) */
+    int32_t warps_per_block;  /* 2, 4 or 8 */
+    int32_t local_stacks;     /* per-ray stacks in local memory (1) or block shared memory (0) */
+    int32_t grid;             /* persistent blocks of its launch */
+    int32_t n_items;          /* its 32-pixel warp tiles */
+    float tuned_ms;           /* the class alone at its tuned configuration; 0 before tuning */
+} csg_batch_class_info;
 
 /* Builds the batch on the current device: views are grouped into tree-size classes (same
  * kernel variant and live-mask size), each with its own view table (most expensive first)
@@ -168,10 +186,18 @@ int csg_batch_destroy(csg_batch* batch);
 int csg_batch_render(csg_batch* batch, void* stream);
 /* Sets the warp tile width of every class (4, 8, 16 or 32 pixels; height 32 / width). */
 int csg_batch_set_tile(csg_batch* batch, int32_t warp_tile_w);
-/* Autotuner: times every warp tile shape for each class alone, keeps each class's fastest,
- * and reports the heaviest class's shape and the whole batch's time.  Synchronous. */
+/* Sets the block shape of every class's launch: 4 warps per block with the per-ray stacks
+ * in shared memory (local_stacks 0) or in local memory (1), or 2 or 8 warps per block with
+ * shared-memory stacks.  Every shape renders the same bytes. */
+int csg_batch_set_shape(csg_batch* batch, int32_t warps_per_block, int32_t local_stacks);
+/* Autotuner, for each class alone: every warp tile shape with the default block shape,
+ * then the other block shapes (warps per block, stack placement) with the best tile;
+ * keeps each class's fastest and reports the heaviest class's tile width and the whole
+ * batch's time.  Synchronous. */
 int csg_batch_tune(csg_batch* batch, void* stream, int32_t* best_tile_w, float* best_ms);
 int csg_batch_get_info(const csg_batch* batch, csg_batch_info* info);
+/* Class k (0 <= k < n_classes, heaviest first) of the batch. */
+int csg_batch_get_class(const csg_batch* batch, int32_t k, csg_batch_class_info* info);
 /* Synchronises `stream`; number of rays of the batch's renders stopped at the iteration
  * cap since the last call (CSG_E_TIMEOUT if any). */
 int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);

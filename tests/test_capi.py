@@ -78,3 +78,15 @@ def test_server_rejects_bad_configs_without_gpu(csg):
     assert lib.csg_server_create(None, None) == csg.CSG_E_ARG
     assert lib.csg_server_submit(None, None, None) == csg.CSG_E_ARG
     assert lib.csg_server_release(None, 1) == csg.CSG_E_ARG
+
+
+def test_batch_entry_points_reject_null_without_gpu(csg):
+    lib = csg.lib()
+    assert lib.csg_batch_set_shape(None, 4, 0) == csg.CSG_E_ARG
+    assert lib.csg_batch_set_tile(None, 8) == csg.CSG_E_ARG
+    info = csg.csg_batch_class_info()
+    assert lib.csg_batch_get_class(None, 0, ctypes.byref(info)) == csg.CSG_E_ARG
+    assert lib.csg_batch_get_info(None, None) == csg.CSG_E_ARG
+    # the structs' layout: eight-byte aligned info, ten four-byte fields per class
+    assert ctypes.sizeof(csg.csg_batch_info) == 48
+    assert ctypes.sizeof(csg.csg_batch_class_info) == 40

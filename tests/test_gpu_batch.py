@@ -1,6 +1,6 @@
 """The batched persistent launch (csg_batch_*) writes, for every view, exactly the bytes a
-per-view csg_render_planes writes -- for every warp tile shape, after autotuning, and on
-graph replay."""
+per-view csg_render_planes writes -- for every warp tile shape, every block shape (warps
+per block, stack placement), after autotuning, and on graph replay."""
 from __future__ import annotations
 
 import numpy as np
@@ -81,6 +81,77 @@ def test_batch_equals_per_view_renders(csg, deep):
     b.close()
     for sc in scenes_:
         sc.close()
+
+
+SHAPES = [(4, False), (2, False), (8, False), (4, True)]
+
+
+@pytest.mark.parametrize("deep", [False, True])
+def test_batch_block_shapes_equal_per_view_renders(csg, deep):
+    """Every block shape, at two tile widths, and the autotuned configuration per class."""
+    import torch
+    torch.cuda.set_device(0)
+    scenes_, views = _views(csg, torch, n_scenes=5, deep=deep, seed=3)
+    ref, out, bviews = [], [], []
+    for sc, cam, light, w, h in views:
+        r = _alloc(torch, w, h)
+        sc.render_ptrs(cam, light, w, h, **{k: v.data_ptr() for k, v in r.items()})
+        ref.append(r)
+        o = _alloc(torch, w, h)
+        out.append(o)
+        bviews.append((sc, cam, light, w, h, {k: v.data_ptr() for k, v in o.items()}))
+    torch.cuda.synchronize()
+    b = csg.Batch(bviews)
+    assert b.info()["n_classes"] == len(b.classes()) >= 1
+
+    def run_and_compare(tag):
+        for o in out:
+            for v in o.values():
+                v.zero_()
+        b.render()
+        b.render()
+        torch.cuda.synchronize()
+        assert b.check() == 0
+        for r, o in zip(ref, out):
+            for k in r:
+                assert torch.equal(r[k], o[k]), (tag, k)
+
+    for warps, local in SHAPES:
+        b.set_shape(warps, local)
+        for tw in (8, 16):
+            b.set_tile(tw)
+            run_and_compare((warps, local, tw))
+            for c in b.classes():
+                assert (c["warps_per_block"], bool(c["local_stacks"]), c["warp_tile_w"]) == (warps, local, tw)
+                assert c["grid"] >= 1 and c["n_items"] >= 1
+    tw, ms = b.tune()
+    assert ms > 0
+    classes = b.classes()
+    assert tw == classes[0]["warp_tile_w"]
+    assert sum(c["n_views"] for c in classes) == len(views)
+    for c in classes:
+        assert (c["warps_per_block"], bool(c["local_stacks"])) in SHAPES
+        assert c["tuned_ms"] > 0
+    info = b.info()
+    assert (info["warps_per_block"], bool(info["local_stacks"])) == (classes[0]["warps_per_block"],
+                                                                      bool(classes[0]["local_stacks"]))
+    run_and_compare("tuned")
+    b.close()
+    for sc in scenes_:
+        sc.close()
+
+
+def test_batch_rejects_bad_shapes(csg):
+    import torch
+    torch.cuda.set_device(0)
+    sc = csg.Scene("Sphere 0 0 0 FF0000 1")
+    o = torch.zeros(16 * 16, dtype=torch.int32, device="cuda")
+    b = csg.Batch([(sc, csg.Camera(), csg.light_dir(), 16, 16, {"rgba8": o.data_ptr()})])
+    for warps, local in ((3, 0), (1, 0), (16, 0), (2, 1), (8, 1), (4, 2)):
+        assert csg.lib().csg_batch_set_shape(b.h, warps, local) == csg.CSG_E_ARG
+    assert csg.lib().csg_batch_set_shape(None, 4, 0) == csg.CSG_E_ARG
+    b.close()
+    sc.close()
 
 
 def test_batch_rejects_bad_views(csg):
