@@ -314,7 +314,7 @@ def run_engine(args):
                           "per_view_launches": b["per_view_launches"]["value"],
                           "batched_vs_per_view": b["batched_vs_per_view"], "ms_per_batch": b["ms_per_step"],
                           "steps": 2, "warmup": 3}
-        srv = run_serving(sub, sub=True, rates=(1000,), n_req=256)
+        srv = run_serving(sub, sub=True, rates=(1000,), n_req=512)
         row = srv["serving"][0]
         res["serving"] = {"workload": WORKLOADS[5], "rate_rps": 1000, "requests": row["requests"],
                           "batched": {k: row["batched"][k] for k in ("p50_ms", "p99_ms", "mrays_s")},
@@ -488,7 +488,7 @@ def _percentile(v, q):
     return float(np.percentile(np.asarray(v), q)) if len(v) else None
 
 
-def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
+def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=512):
     """Configuration 5: the render server under open-loop Poisson arrivals, with continuous
     batching and with one single-view launch per request (the same server, requests
     flagged CSG_REQ_ALONE), at swept arrival rates.  Latency = completion - scheduled
@@ -511,13 +511,17 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
     rng = np.random.default_rng(5)
     sizes = [256, 512, 1024, 2048]
 
-    def make_requests(n, alone, with_host=False):
+    def make_spec(n):
         r2 = np.random.default_rng(rng.integers(1 << 31))
         spec = []
         for _ in range(n):
             sid = int(r2.integers(0, n_pool))
             res = sizes[int(r2.integers(0, 4))]
             spec.append((sid, res, csgrt.Camera.look_at_origin(S.seeded_direction(r2), 4.0, 60.0)))
+        return spec
+
+    def make_requests(spec, alone, with_host=False):
+        """The requests of `spec`, served batched or one launch each (alone)."""
         rays = sum(res * res for _, res, _ in spec)
         host = torch.empty(rays, dtype=torch.int32, pin_memory=True) if with_host else None
         out, offs = [], 0
@@ -529,8 +533,9 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
 
     # warm-up: both forms, every kernel variant the pool needs
     for _ in range(args.warmup):
+        spec = make_spec(24)
         for alone in (False, True):
-            reqs, _, _ = make_requests(24, alone)
+            reqs, _, _ = make_requests(spec, alone)
             srv.replay(reqs, np.zeros(len(reqs)))
     rates = list(rates)
     sweep = []
@@ -540,8 +545,9 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
             row = {"rate_rps": rate, "requests": n_req}
             arrivals = np.cumsum(np.random.default_rng(rate).exponential(1.0 / rate, n_req))
             arrivals -= arrivals[0]
+            spec = make_spec(n_req)  # both forms serve the same requests at the same arrival times
             for alone in (False, True):
-                reqs, rays, _ = make_requests(n_req, alone)
+                reqs, rays, _ = make_requests(spec, alone)
                 b0 = srv.stats()["batches"]
                 res, _, wall = srv.replay(reqs, arrivals)
                 launches += srv.stats()["batches"] - b0
@@ -558,7 +564,7 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=256):
         top = rates[-1]
         arrivals = np.cumsum(np.random.default_rng(top).exponential(1.0 / top, n_req))
         arrivals -= arrivals[0]
-        reqs, rays_e2e, host = make_requests(n_req, False, with_host=True)
+        reqs, rays_e2e, host = make_requests(make_spec(n_req), False, with_host=True)
         res, _, wall_e2e = srv.replay(reqs, arrivals)
         lat_e2e = [1000.0 * (r.t_done - r.t_arrive) for r in res]
     top_row = sweep[-1]

@@ -4,7 +4,7 @@ enough to run under a profiler.
 
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 2 --repeat 2
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 3 --seed 4 --png out.png
-    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2 --local-stacks
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scene 191 --view-width 1024
 
 Configurations: 1 the README tree at 1280x720, 2 the 512-sphere cheese at 3840x2160,
@@ -34,6 +34,9 @@ def main(argv=None):
     ap.add_argument("--batch-scenes", type=int, default=0, help="render the first N batch scenes x 4 views")
     ap.add_argument("--batch-scene", type=int, default=-1, help="render one scene of the batched workload")
     ap.add_argument("--view-width", type=int, default=0, help="with --batch-scene: its view of this size")
+    ap.add_argument("--tile", type=int, default=8, help="with --batch-scenes: warp tile width (4, 8, 16, 32)")
+    ap.add_argument("--warps", type=int, default=4, help="with --batch-scenes: warps per block (2, 4, 8)")
+    ap.add_argument("--local-stacks", action="store_true", help="with --batch-scenes: per-ray stacks in local memory")
     ap.add_argument("--png", default="", help="write the (single-view) frame as PNG")
     ap.add_argument("--ppm", default="", help="write the (single-view) frame as PPM")
     a = ap.parse_args(argv)
@@ -51,10 +54,14 @@ def main(argv=None):
                 outs.append(o)
                 views.append((sc, csgrt.Camera.from_floats(v.camera), v.light, v.w, v.h, {"rgba8": o.data_ptr()}))
         b = csgrt.Batch(views)
+        b.set_tile(a.tile)
+        b.set_shape(a.warps, a.local_stacks)
         for _ in range(a.repeat):
             b.render()
         torch.cuda.synchronize()
         print("batch", b.info())
+        for k, c in enumerate(b.classes()):
+            print("class", k, c)
         return 0
 
     if a.batch_scene >= 0:
