@@ -42,6 +42,7 @@ EXPORTED = [
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
     "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex", "csg_batch_set_shape", "csg_batch_get_class",
+    "csg_render_host",
 ]
 
 _vp = ctypes.c_void_p
@@ -156,6 +157,7 @@ def lib() -> ctypes.CDLL:
     L.csg_render.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp, _vp, _vp, _vp]
     L.csg_render_f4.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
     L.csg_render_planes.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, ctypes.POINTER(csg_planes), _vp]
+    L.csg_render_host.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
     L.csg_scene_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_device_tan_half_fov.argtypes = [_f, ctypes.POINTER(_f)]
     L.csg_probe_fp32_peak.argtypes = [ctypes.POINTER(_f), ctypes.POINTER(_f)]
@@ -356,6 +358,12 @@ class Scene:
         pl = csg_planes(rgba8 or None, rgba32f or None, t or None, prim or None, normal or None)
         check(lib().csg_render_planes(self.h, ctypes.byref(cam.c), light, w, h, ctypes.byref(pl),
                                       stream or None))
+
+    def render_host(self, cam: Camera, light, w: int, h: int, host_rgba8: int, stream=0):
+        """RGBA8 frame into host memory at address `host_rgba8` (csg_render_host): written by
+        the kernel itself when page-locked, staged through the device otherwise."""
+        light = (_f * 3)(*[float(v) for v in light])
+        check(lib().csg_render_host(self.h, ctypes.byref(cam.c), light, w, h, host_rgba8, stream or None))
 
     def render_torch(self, cam: Camera, light, w: int, h: int, planes=("rgba8",), stream=None, out=None):
         """Render into torch CUDA tensors; returns a dict of the requested planes."""

@@ -361,6 +361,34 @@ int csg_render_planes(const csg_scene* s, const csg_camera* cam, const float lig
     return render_common(s, cam, light_dir, w, h, p, stream);
 }
 
+int csg_render_host(const csg_scene* s, const csg_camera* cam, const float light_dir[3], int32_t w, int32_t h,
+                    uint32_t* host_rgba8, void* stream)
+{
+    if (!s || !cam || !light_dir || !host_rgba8 || w <= 0 || h <= 0) return CSG_E_ARG;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaPointerAttributes a{};
+    const cudaError_t qe = cudaPointerGetAttributes(&a, host_rgba8);
+    cudaGetLastError();  // an unregistered pointer may leave an error behind on older runtimes
+    if (qe == cudaSuccess && (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged))
+        return CSG_E_ARG;  // a device buffer: csg_render writes it
+    csgrt::Planes p;
+    if (qe == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer) {
+        // page-locked and mapped: the kernel stores the frame into host memory itself
+        p.rgba8 = static_cast<uint32_t*>(a.devicePointer);
+        return render_common(s, cam, light_dir, w, h, p, stream);
+    }
+    // pageable: a stream-ordered device frame, then a copy (which returns when done)
+    const size_t bytes = (size_t)w * (size_t)h * sizeof(uint32_t);
+    void* d = nullptr;
+    if (cudaMallocAsync(&d, bytes, st) != cudaSuccess) return CSG_E_CUDA;
+    p.rgba8 = static_cast<uint32_t*>(d);
+    int rc = render_common(s, cam, light_dir, w, h, p, stream);
+    if (rc == CSG_OK && cudaMemcpyAsync(host_rgba8, d, bytes, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+        rc = CSG_E_CUDA;
+    if (cudaFreeAsync(d, st) != cudaSuccess && rc == CSG_OK) rc = CSG_E_CUDA;
+    return rc;
+}
+
 int csg_device_tan_half_fov(float fov, float* out)
 {
     if (!out) return CSG_E_ARG;

@@ -130,6 +130,14 @@ int csg_render_f4(const csg_scene* scene, const csg_camera* cam, const float lig
 /* Every plane at once. */
 int csg_render_planes(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
                       int32_t w, int32_t h, const csg_planes* planes, void* stream);
+/* No counterpart in the reference (whose frame stays in a device PBO): renders the RGBA8
+ * frame into HOST memory.  A page-locked destination (cudaHostAlloc, cudaMallocHost,
+ * cudaHostRegister) is written by the kernel itself over the host link, with no staging
+ * buffer and no separate copy, and the call is asynchronous on `stream`; a pageable
+ * destination is rendered into a stream-ordered device frame and copied, and the call
+ * returns once the frame is in host memory.  A device pointer is CSG_E_ARG. */
+int csg_render_host(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
+                    int32_t w, int32_t h, uint32_t* host_rgba8, void* stream);
 /* Synchronises `stream` and reports how many rays of the renders issued since the last
  * call stopped at the traversal iteration cap (CSG_E_TIMEOUT if any, else CSG_OK). */
 int csg_scene_check(const csg_scene* scene, void* stream, uint64_t* n_capped);

@@ -90,3 +90,11 @@ def test_batch_entry_points_reject_null_without_gpu(csg):
     # the structs' layout: eight-byte aligned info, ten four-byte fields per class
     assert ctypes.sizeof(csg.csg_batch_info) == 48
     assert ctypes.sizeof(csg.csg_batch_class_info) == 40
+
+
+def test_host_render_rejects_null_without_gpu(csg):
+    lib = csg.lib()
+    cam = csg.Camera()
+    light = (ctypes.c_float * 3)(-1, -1, -1)
+    buf = (ctypes.c_uint32 * 4)()
+    assert lib.csg_render_host(None, ctypes.byref(cam.c), light, 2, 2, ctypes.addressof(buf), None) == csg.CSG_E_ARG
