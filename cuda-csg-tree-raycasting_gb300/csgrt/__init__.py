@@ -42,7 +42,7 @@ EXPORTED = [
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
     "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex", "csg_batch_set_shape", "csg_batch_get_class",
-    "csg_render_host",
+    "csg_render_host", "csg_batch_set_class",
 ]
 
 _vp = ctypes.c_void_p
@@ -169,6 +169,7 @@ def lib() -> ctypes.CDLL:
     L.csg_batch_get_info.argtypes = [_vp, ctypes.POINTER(csg_batch_info)]
     L.csg_batch_set_shape.argtypes = [_vp, _i32, _i32]
     L.csg_batch_get_class.argtypes = [_vp, _i32, ctypes.POINTER(csg_batch_class_info)]
+    L.csg_batch_set_class.argtypes = [_vp, _i32, _i32, _i32, _i32]
     L.csg_batch_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_render_views_noalloc.argtypes = [ctypes.POINTER(csg_view), _i32, _i32, _vp]
     L.csg_server_create.argtypes = [ctypes.POINTER(csg_server_config), ctypes.POINTER(_vp)]
@@ -433,6 +434,20 @@ class Batch:
     def set_shape(self, warps_per_block: int = 4, local_stacks: bool = False):
         """Block shape of every class's launch: (4, False), (4, True), (2, False) or (8, False)."""
         check(lib().csg_batch_set_shape(self.h, warps_per_block, int(bool(local_stacks))))
+
+    def set_class(self, k: int, warp_tile_w: int, warps_per_block: int = 4, local_stacks: bool = False):
+        """Class k's warp tile width and block shape."""
+        check(lib().csg_batch_set_class(self.h, k, warp_tile_w, warps_per_block, int(bool(local_stacks))))
+
+    def copy_config(self, other: "Batch"):
+        """Gives every class the configuration of the same class of `other` (a batch over the
+        same scenes, e.g. one that was tuned)."""
+        mine, theirs = self.classes(), other.classes()
+        if [(c["stack_class"], c["rolled"], c["live_words"], c["n_views"]) for c in mine] != \
+                [(c["stack_class"], c["rolled"], c["live_words"], c["n_views"]) for c in theirs]:
+            raise ValueError("batches have different tree-size classes")
+        for k, c in enumerate(theirs):
+            self.set_class(k, c["warp_tile_w"], c["warps_per_block"], bool(c["local_stacks"]))
 
     def classes(self) -> list:
         """Per tree-size class (heaviest first): its kernel variant and configuration."""

@@ -186,7 +186,9 @@ typedef struct csg_batch_class_info {
 /* Builds the batch on the current device: views are grouped into tree-size classes (same
  * kernel variant and live-mask size), each with its own view table (most expensive first)
  * and persistent launch.  The scenes and the output planes must stay valid while the
- * batch is used. */
+ * batch is used.  Output planes may be device memory or page-locked host memory, which
+ * the kernel writes over the host link (the frames are complete when the render's stream
+ * is); pageable host memory is CSG_E_ARG. */
 int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out);
 int csg_batch_destroy(csg_batch* batch);
 /* Renders every view: one CUDA graph, captured on the first call (and again after a tile
@@ -206,6 +208,11 @@ int csg_batch_tune(csg_batch* batch, void* stream, int32_t* best_tile_w, float* 
 int csg_batch_get_info(const csg_batch* batch, csg_batch_info* info);
 /* Class k (0 <= k < n_classes, heaviest first) of the batch. */
 int csg_batch_get_class(const csg_batch* batch, int32_t k, csg_batch_class_info* info);
+/* Sets class k's warp tile width and block shape (as csg_batch_set_tile and
+ * csg_batch_set_shape do for every class), e.g. to give a second batch over the same
+ * scenes the configuration another batch was tuned to. */
+int csg_batch_set_class(csg_batch* batch, int32_t k, int32_t warp_tile_w, int32_t warps_per_block,
+                        int32_t local_stacks);
 /* Synchronises `stream`; number of rays of the batch's renders stopped at the iteration
  * cap since the last call (CSG_E_TIMEOUT if any). */
 int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);

@@ -98,3 +98,7 @@ def test_host_render_rejects_null_without_gpu(csg):
     light = (ctypes.c_float * 3)(-1, -1, -1)
     buf = (ctypes.c_uint32 * 4)()
     assert lib.csg_render_host(None, ctypes.byref(cam.c), light, 2, 2, ctypes.addressof(buf), None) == csg.CSG_E_ARG
+
+
+def test_batch_class_setter_rejects_null_without_gpu(csg):
+    assert csg.lib().csg_batch_set_class(None, 0, 8, 4, 0) == csg.CSG_E_ARG

@@ -160,3 +160,54 @@ def test_batch_rejects_bad_views(csg):
     h = ctypes.c_void_p()
     assert csg.lib().csg_batch_create(arr, 1, ctypes.byref(h)) == csg.CSG_E_ARG
     assert csg.lib().csg_batch_create(arr, 0, ctypes.byref(h)) == csg.CSG_E_ARG
+
+
+def test_batch_writes_page_locked_host_planes(csg):
+    """Views whose planes are page-locked host memory: the kernel writes them directly, the
+    bytes equal the device renders; a copied configuration (copy_config) is the tuned one;
+    pageable host planes are refused."""
+    import ctypes
+    import torch
+    torch.cuda.set_device(0)
+    scenes_, views = _views(csg, torch, n_scenes=4, seed=7)
+    ref, dev_views, host_out, host_views = [], [], [], []
+    for sc, cam, light, w, h in views:
+        r = _alloc(torch, w, h)
+        sc.render_ptrs(cam, light, w, h, **{k: v.data_ptr() for k, v in r.items()})
+        ref.append(r)
+        dev_views.append((sc, cam, light, w, h, {"rgba8": r["rgba8"].data_ptr()}))
+        o = {"rgba8": torch.zeros(w * h, dtype=torch.int32, pin_memory=True),
+             "t": torch.zeros(w * h, dtype=torch.float32, pin_memory=True)}
+        host_out.append(o)
+        host_views.append((sc, cam, light, w, h, {k: v.data_ptr() for k, v in o.items()}))
+    torch.cuda.synchronize()
+    tuned = csg.Batch(dev_views)
+    tuned.tune()
+    b = csg.Batch(host_views)
+    b.copy_config(tuned)
+    for mine, theirs in zip(b.classes(), tuned.classes()):
+        for k in ("warp_tile_w", "warps_per_block", "local_stacks"):
+            assert mine[k] == theirs[k]
+    b.render()
+    torch.cuda.synchronize()
+    assert b.check() == 0
+    for r, o in zip(ref, host_out):
+        assert torch.equal(r["rgba8"].cpu(), o["rgba8"])
+        assert torch.equal(r["t"].cpu(), o["t"])
+    b.close()
+    tuned.close()
+    # pageable host memory cannot be written by a kernel
+    import numpy as np
+    sc, cam, light, w, h = views[0]
+    page = np.zeros(w * h, dtype=np.int32)
+    arr = (csg.csg_view * 1)()
+    arr[0].scene = sc.h
+    ctypes.memmove(ctypes.byref(arr[0].cam), ctypes.byref(cam.c), 60)
+    for k in range(3):
+        arr[0].light_dir[k] = float(light[k])
+    arr[0].w, arr[0].h = w, h
+    arr[0].out = csg.csg_planes(page.ctypes.data, None, None, None, None)
+    hb = ctypes.c_void_p()
+    assert csg.lib().csg_batch_create(arr, 1, ctypes.byref(hb)) == csg.CSG_E_ARG
+    for sc in scenes_:
+        sc.close()
