@@ -12,7 +12,14 @@ namespace csgrt {
 namespace {
 
 using pix::kThreads;
-constexpr int kTileW = 16, kTileH = 8;
+// Warp tile (a tuning knob): CSG_TILED_WARP_W x (32 / CSG_TILED_WARP_W) pixels; a block's
+// four warps form a 2 x 2 arrangement of warp tiles.
+#ifndef CSG_TILED_WARP_W
+#define CSG_TILED_WARP_W 8
+#endif
+constexpr int kWarpW = CSG_TILED_WARP_W, kWarpH = 32 / CSG_TILED_WARP_W;
+constexpr int kTileW = 2 * kWarpW, kTileH = 2 * kWarpH;
+static_assert(kWarpW == 4 || kWarpW == 8 || kWarpW == 16, "warp tile width");
 
 struct RenderParams {
     pix::ViewParams view;
@@ -50,8 +57,8 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     else st = pix::block_stacks<SD, kThreads>(smem_raw);
     const pix::BlockSmem bs = pix::block_smem<SD, kThreads, kLocalStacks>(smem_raw, p.view.scene.live_words);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
-    const int y = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
+    const int x = blockIdx.x * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
+    const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
     pix::render_pixel<SD, ROLLED>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st, bs, tab);
 }
