@@ -8,6 +8,7 @@
 // behaviour) this parser reports CSG_E_PARSE instead.
 #include "scene.hpp"
 
+#include <algorithm>
 #include <cerrno>
 #include <cmath>
 #include <cstdlib>
@@ -490,20 +491,31 @@ struct BvhBuilder {
 void pack_scene(const HostTree& t, PackedScene& out)
 {
     const size_t n = t.nodes.size(), np = t.prims.size();
+    // Device node numbering: the operators first, in preorder (the root, node 0 of the
+    // reference, stays 0), then the leaves.  Only operators have kids records, so those are
+    // dense and a cache line holds only records the traversal reads.
+    std::vector<int32_t> num(n, -1);
+    int32_t next = 0;
+    for (size_t i = 0; i < n; ++i)
+        if (t.nodes[i].prim == -1 || !CSG_DENSE_OPERATORS) num[i] = next++;
+    const size_t n_ops = static_cast<size_t>(CSG_DENSE_OPERATORS ? next : n);
+    for (size_t i = 0; i < n; ++i)
+        if (num[i] < 0) num[i] = next++;
+    auto dev = [&](int32_t old) { return old < 0 ? old : num[old]; };
     out.topo.assign(n, int4{0, 0, 0, 0});
-    out.kids.assign(kKidsPerNode * n, float4{0, 0, 0, 0});
+    out.kids.assign(kKidsPerNode * std::max<size_t>(n_ops, 1), float4{0, 0, 0, 0});
     out.geo.assign(2 * np, float4{0, 0, 0, 0});
     out.color.assign(np, float4{0, 0, 0, 0});
     for (size_t i = 0; i < n; ++i) {
         const RefNode& nd = t.nodes[i];
         if (nd.prim != -1) {
-            out.topo[i] = int4{nd.prim, -1, nd.parent, nd.type};
+            out.topo[num[i]] = int4{nd.prim, -1, dev(nd.parent), nd.type};
             continue;
         }
-        out.topo[i] = int4{nd.left, nd.right, nd.parent, nd.type};
+        out.topo[num[i]] = int4{dev(nd.left), dev(nd.right), dev(nd.parent), nd.type};
         const RefNode& l = t.nodes[nd.left];
         const RefNode& r = t.nodes[nd.right];
-        float4* k = &out.kids[kKidsPerNode * i];
+        float4* k = &out.kids[kKidsPerNode * num[i]];
         k[0] = float4{l.minx, l.miny, l.minz, as_float(l.type)};
         k[1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
         k[2] = float4{r.minx, r.miny, r.minz, as_float(r.type)};

@@ -52,8 +52,9 @@ void use_exact_boxes(HostTree& t);
 // ---------------------------------------------------------------------------------
 // Device layout (all arrays 16-byte aligned, one cudaMalloc):
 //   topo[n]    int4   {left, right, parent, type} for operators,
-//                     {prim, -1, parent, type} for leaves
-//   kids[5n]   for an operator node, everything GoTo needs in five independent 16-byte
+//                     {prim, -1, parent, type} for leaves (device node numbers: see
+//                     CSG_DENSE_OPERATORS)
+//   kids[5m]   for each of the m operator nodes, everything GoTo needs in five independent 16-byte
 //                     loads (the Ulyanov layout): the two children's boxes with the
 //                     child's type and primitive index in .w (as int bits), then the
 //                     children's leaf ranges:
@@ -68,6 +69,12 @@ void use_exact_boxes(HostTree& t);
 //                     child >= 0 is a BVH node and child < 0 is leaf ~prim (type valid)
 // ---------------------------------------------------------------------------------
 constexpr int kKidsPerNode = 5;
+// Node numbering of the device arrays (a build-time knob): 1 numbers the operators first
+// (kids records dense, one per operator), 0 keeps the reference's preorder (a kids record
+// per node, zeros for leaves).  Either way node 0 is the root.
+#ifndef CSG_DENSE_OPERATORS
+#define CSG_DENSE_OPERATORS 1
+#endif
 // Live-leaf mask: at most CSG_LIVE_WORDS_MAX words per ray (32: 1024 bits; 64 is the
 // largest the one-register word summary can index).  A build-time tuning knob: more words
 // keep one bit per leaf on larger trees at the cost of shared memory per block.
