@@ -44,6 +44,14 @@ struct RenderParams {
 #define CSG_TILED_LOCAL_STACKS 0
 #endif
 constexpr bool kLocalStacks = CSG_TILED_LOCAL_STACKS != 0;
+// Preferred shared-memory carveout in percent of the maximum (a tuning knob; -1 leaves
+// the choice to the driver, which sizes shared memory for the most resident blocks).
+// 80% keeps six blocks per SM for live masks up to ~30 KB per block and gives the largest
+// masks five blocks and a larger L1: 5% faster on the heaviest batch view (1,694 leaves,
+// whose 0.5 MB scene misses L1), within 1% elsewhere; 66% and 50% cost up to 11% and 35%.
+#ifndef CSG_TILED_CARVEOUT
+#define CSG_TILED_CARVEOUT 80
+#endif
 
 template <int SD, bool ROLLED>
 __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG_UNROLLED_MIN_BLOCKS)
@@ -71,10 +79,11 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
     // largest layout any scene can ask for (kLiveWordsMax live words).
     static bool attr_set = false;
     if (!attr_set) {
-        const cudaError_t e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads,
-                                                                        kLocalStacks));
+        cudaError_t e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads, kLocalStacks));
+        if (e == cudaSuccess && CSG_TILED_CARVEOUT >= 0)
+            e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     CSG_TILED_CARVEOUT);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
