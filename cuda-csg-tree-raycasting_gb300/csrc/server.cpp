@@ -13,11 +13,13 @@
 //
 // Completion.  Requests retire one by one, not per batch: the block that renders a view's
 // last tile fences its writes system-wide and stores the batch's epoch into that view's
-// host-mapped flag, and a poller thread turns flags into completed requests.  A host
-// function enqueued after the kernel (it makes no CUDA call) frees the slot, settles the
-// budget and completes any request still open (one whose RGBA8 plane is copied to a
-// pageable host buffer after the kernel).  An RGBA8 destination in pinned host memory is
-// written by the kernel directly.  Requests flagged CSG_REQ_ALONE are launched one by one
+// host-mapped flag, and a poller thread turns flags into completed requests.  An event
+// recorded after each launch's last operation tells the same poller (cudaEventQuery, no
+// waiting) when the whole launch is over; it then frees the slot, settles the budget and
+// completes any request still open (one whose RGBA8 plane is copied to a pageable host
+// buffer after the kernel).  The poller wakes every 20 us while launches are in flight,
+// which answers sooner than a host function enqueued on the stream.  An RGBA8
+// destination in pinned host memory is written by the kernel directly.  Requests flagged CSG_REQ_ALONE are launched one by one
 // with the single-view kernel on one stream, in arrival order: the unbatched form.
 //
 // Budget.  Resident scenes and the output planes of admitted, unreleased requests count
@@ -36,6 +38,10 @@
 #include <thread>
 #include <unordered_map>
 #include <vector>
+
+#if defined(__linux__)
+#include <sys/prctl.h>
+#endif
 
 #include "csgrt.h"
 #include "scene.hpp"
@@ -83,12 +89,12 @@ struct PoolScene {
 
 struct Slot {
     cudaStream_t stream = nullptr;
-    void* dmem = nullptr;                 // view table, prefix, remaining tiles, counter
+    void* dmem = nullptr;                 // counter, prefix, remaining tiles, view table
     csgrt::ViewRecord* d_views = nullptr;
     int32_t* d_prefix = nullptr;
     int32_t* d_remaining = nullptr;
     int* d_counter = nullptr;
-    void* hmem = nullptr;                 // pinned staging of table, prefix and remaining
+    void* hmem = nullptr;                 // pinned staging of the same layout
     csgrt::ViewRecord* h_views = nullptr;
     int32_t* h_prefix = nullptr;
     int32_t* h_remaining = nullptr;
@@ -103,6 +109,7 @@ struct Launch {
     int slot;                // -1: an unbatched launch
     unsigned int epoch;
     std::vector<Req*> reqs;  // in view-table order
+    cudaEvent_t done = nullptr;  // recorded after the launch's last operation
 };
 
 size_t up_align(size_t v)
@@ -165,8 +172,10 @@ struct csg_server {
     std::unordered_map<int64_t, Req*> reqs;
     std::vector<PoolScene> scenes;
     Slot slots[kMaxSlots];
-    std::list<Launch*> tracked;       // batched launches whose flags the poller watches
+    std::list<Launch*> tracked;       // launches in flight, watched by the poller
+    std::vector<cudaEvent_t> events;  // completion events not in use
     cudaStream_t alone = nullptr;     // stream of the unbatched launches
+    size_t table_head = 0;            // bytes before a slot's view records
     cudaMemPool_t pool = nullptr;
     uint64_t scene_bytes = 0, output_bytes = 0, peak = 0, use_clock = 0;
     int64_t next_ticket = 1, n_done = 0, n_batches = 0, n_evict = 0, n_rejected = 0;
@@ -197,22 +206,13 @@ struct csg_server {
     void finish(Launch* L, int status);
 };
 
-namespace {
-
-void on_done(void* p)
-{
-    Launch* L = static_cast<Launch*>(p);
-    L->srv->finish(L, CSG_OK);
-}
-
-}  // namespace
-
-// End of a launch: runs on a CUDA host-function thread (no CUDA calls here), or on the
-// dispatcher when a launch could not be enqueued.
+// End of a launch: runs on the poller once the launch's event has completed, or on the
+// dispatcher when a launch could not be enqueued (no CUDA calls here).
 void csg_server::finish(Launch* L, int status)
 {
     {
         std::lock_guard<std::mutex> lk(mu);
+        if (L->done) events.push_back(L->done);
         const double t = now();
         for (Req* q : L->reqs) {
             if (q->status == CSG_OK) q->status = status;
@@ -230,10 +230,7 @@ void csg_server::finish(Launch* L, int status)
             }
             if (q->released) delete q;
         }
-        if (L->slot >= 0) {
-            slots[L->slot].busy = false;
-            tracked.remove(L);
-        }
+        if (L->slot >= 0) slots[L->slot].busy = false;
         --in_flight;
         ++gen;
     }
@@ -244,13 +241,22 @@ void csg_server::finish(Launch* L, int status)
 
 void csg_server::poll_loop()
 {
+#if defined(__linux__) && defined(PR_SET_TIMERSLACK)
+    // This thread's sleeps between polls are 20 us; the default 50 us timer slack would
+    // add up to that much to every completion.
+    prctl(PR_SET_TIMERSLACK, 1000UL, 0UL, 0UL, 0UL);
+#endif
+    cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(mu);
+    std::vector<Launch*> watch, ended;
+    std::vector<int> ended_status;
     while (true) {
         cv_poll.wait(lk, [&] { return stop_poll || !tracked.empty(); });
         if (tracked.empty()) break;  // stop_poll
         bool any = false;
         const double t = now();
         for (Launch* L : tracked) {
+            if (L->slot < 0) continue;
             const volatile unsigned int* f = slots[L->slot].h_flags;
             for (size_t k = 0; k < L->reqs.size(); ++k) {
                 Req* q = L->reqs[k];
@@ -261,8 +267,27 @@ void csg_server::poll_loop()
             }
         }
         if (any) cv_done.notify_all();
+        // Launches end only here, so the ones in `watch` stay valid without the lock.
+        watch.assign(tracked.begin(), tracked.end());
         lk.unlock();
-        std::this_thread::sleep_for(std::chrono::microseconds(20));
+        ended.clear();
+        ended_status.clear();
+        for (Launch* L : watch) {
+            const cudaError_t e = cudaEventQuery(L->done);
+            if (e == cudaErrorNotReady) continue;
+            ended.push_back(L);
+            ended_status.push_back(e == cudaSuccess ? CSG_OK : CSG_E_CUDA);
+        }
+        if (!ended.empty()) {
+            cudaGetLastError();
+            {
+                std::lock_guard<std::mutex> g(mu);
+                for (Launch* L : ended) tracked.remove(L);
+            }
+            for (size_t i = 0; i < ended.size(); ++i) finish(ended[i], ended_status[i]);
+        } else {
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+        }
         lk.lock();
     }
 }
@@ -411,13 +436,9 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
             }
             const size_t nv = batch.size();
             S.h_prefix[nv] = (int32_t)total;
-            const size_t nv_max = (size_t)cfg.max_batch_views;
-            e = cudaMemcpyAsync(S.d_views, S.h_views, nv * sizeof(csgrt::ViewRecord), cudaMemcpyHostToDevice, st);
-            // prefix (nv_max + 1 words) and remaining (nv_max words) are contiguous
-            if (e == cudaSuccess)
-                e = cudaMemcpyAsync(S.d_prefix, S.h_prefix, (2 * nv_max + 1) * sizeof(int32_t),
-                                    cudaMemcpyHostToDevice, st);
-            if (e == cudaSuccess) e = cudaMemsetAsync(S.d_counter, 0, sizeof(int), st);
+            // counter (0), prefix, remaining and the batch's view records in one copy
+            e = cudaMemcpyAsync(S.dmem, S.hmem, table_head + nv * sizeof(csgrt::ViewRecord), cudaMemcpyHostToDevice,
+                                st);
             if (e == cudaSuccess) {
                 csgrt::ViewsLaunch vl;
                 vl.views = S.d_views;
@@ -450,13 +471,19 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
     if (rc == CSG_OK && e == cudaSuccess) {
         {
             std::lock_guard<std::mutex> g(mu);
-            if (!alone_form) tracked.push_back(L);
+            if (!events.empty()) {
+                L->done = events.back();
+                events.pop_back();
+            }
         }
-        cv_poll.notify_one();
-        e = cudaLaunchHostFunc(st, on_done, L);
-        if (e != cudaSuccess) {
-            std::lock_guard<std::mutex> g(mu);
-            tracked.remove(L);
+        if (!L->done) e = cudaEventCreateWithFlags(&L->done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(L->done, st);
+        if (e == cudaSuccess) {
+            {
+                std::lock_guard<std::mutex> g(mu);
+                tracked.push_back(L);
+            }
+            cv_poll.notify_one();
         }
     }
     if (rc != CSG_OK || e != cudaSuccess) {
@@ -572,9 +599,12 @@ int csg_server_create(const csg_server_config* cfg_in, csg_server** out)
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->alone, cudaStreamNonBlocking);
     const size_t nv = (size_t)cfg.max_batch_views;
-    // [views][prefix: nv + 1][remaining: nv][counter], the same layout staged on the host
-    const size_t tab = nv * sizeof(csgrt::ViewRecord) + (2 * nv + 1) * sizeof(int32_t);
-    const size_t dbytes = ((tab + 15) & ~size_t(15)) + 16;
+    // [counter | pad to 16][prefix: nv + 1][remaining: nv][pad to 16][views], the same
+    // layout staged on the host, so that one copy (its length set by the views in the
+    // batch) resets the counter and carries the whole table
+    const size_t head = (16 + (2 * nv + 1) * sizeof(int32_t) + 15) & ~size_t(15);
+    const size_t dbytes = head + nv * sizeof(csgrt::ViewRecord);
+    s->table_head = head;
     for (int i = 0; i < cfg.slots && e == cudaSuccess; ++i) {
         Slot& S = s->slots[i];
         e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking);
@@ -585,13 +615,14 @@ int csg_server_create(const csg_server_config* cfg_in, csg_server** out)
         if (e == cudaSuccess) e = cudaHostGetDevicePointer(reinterpret_cast<void**>(&S.d_flags), S.h_flags, 0);
         if (e != cudaSuccess) break;
         std::memset(S.h_flags, 0, nv * sizeof(unsigned int));
-        S.d_views = static_cast<csgrt::ViewRecord*>(S.dmem);
-        S.d_prefix = reinterpret_cast<int32_t*>(S.d_views + nv);
+        std::memset(S.hmem, 0, head);  // the staged counter stays 0
+        S.d_counter = static_cast<int*>(S.dmem);
+        S.d_prefix = reinterpret_cast<int32_t*>(static_cast<char*>(S.dmem) + 16);
         S.d_remaining = S.d_prefix + nv + 1;
-        S.d_counter = reinterpret_cast<int*>(static_cast<char*>(S.dmem) + dbytes - 16);
-        S.h_views = static_cast<csgrt::ViewRecord*>(S.hmem);
-        S.h_prefix = reinterpret_cast<int32_t*>(S.h_views + nv);
+        S.d_views = reinterpret_cast<csgrt::ViewRecord*>(static_cast<char*>(S.dmem) + head);
+        S.h_prefix = reinterpret_cast<int32_t*>(static_cast<char*>(S.hmem) + 16);
         S.h_remaining = S.h_prefix + nv + 1;
+        S.h_views = reinterpret_cast<csgrt::ViewRecord*>(static_cast<char*>(S.hmem) + head);
     }
     if (e != cudaSuccess) {
         csg_server_destroy(s);
@@ -614,7 +645,7 @@ int csg_server_destroy(csg_server* s)
         s->cv_work.notify_all();
         s->dispatcher.join();
     }
-    // wait for every launch (their host functions touch the server)
+    // wait for every launch (the poller finishes them)
     {
         std::unique_lock<std::mutex> lk(s->mu);
         s->cv_done.wait(lk, [&] { return s->in_flight == 0; });
@@ -640,6 +671,7 @@ int csg_server_destroy(csg_server* s)
         if (S.h_flags) cudaFreeHost(S.h_flags);
     }
     if (s->alone) cudaStreamDestroy(s->alone);
+    for (cudaEvent_t ev : s->events) cudaEventDestroy(ev);
     if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return CSG_OK;
