@@ -5,6 +5,7 @@
 #pragma once
 
 #include <algorithm>
+#include <mutex>
 
 #include "pixel.cuh"
 #include "views.hpp"
@@ -76,14 +77,45 @@ cudaError_t launch_views_variant(const ViewsLaunch& l, int device, cudaStream_t 
 {
     const auto kernel = render_views<SD, ROLLED, NT, LOCAL>;
     const size_t smem = pix::smem_bytes(SD, l.live_words, NT, LOCAL);
-    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    int sms = 0, per_sm = 0;
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, smem);
-    if (e != cudaSuccess) return e;
+    // Resident blocks of the whole device for each (device, live-mask size), found once:
+    // the opt-in for the largest shared-memory layout, the SM count and the occupancy query
+    // cost more host time than the launch itself.  A fixed table (no heap allocation, for
+    // the allocation-free entry point); keys that do not fit are recomputed every time.
+    constexpr int kEntries = 64;
+    static std::mutex mu;
+    static int keys[kEntries];  // device * 256 + live words + 1; 0 = empty
+    static int slots_of[kEntries];
+    const int key = device * 256 + (int)l.live_words + 1;
+    int slots = 0;
+    {
+        std::lock_guard<std::mutex> g(mu);
+        int free_at = -1;
+        for (int i = 0; i < kEntries; ++i) {
+            if (keys[i] == key) {
+                slots = slots_of[i];
+                break;
+            }
+            if (keys[i] == 0) {
+                free_at = i;
+                break;
+            }
+        }
+        if (slots == 0) {
+            cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)pix::smem_bytes(SD, kLiveWordsMax, NT, LOCAL));
+            int sms = 0, per_sm = 0;
+            if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+            if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, NT, smem);
+            if (e != cudaSuccess) return e;
+            slots = sms * std::max(per_sm, 1);
+            if (free_at >= 0) {
+                keys[free_at] = key;
+                slots_of[free_at] = slots;
+            }
+        }
+    }
     // one block per resident slot, but no more warps than items
-    int grid = sms * std::max(per_sm, 1);
-    grid = std::max(1, std::min(grid, (l.n_items + NT / 32 - 1) / (NT / 32)));
+    const int grid = std::max(1, std::min(slots, (l.n_items + NT / 32 - 1) / (NT / 32)));
     if (grid_out) {
         *grid_out = grid;
         return cudaSuccess;
