@@ -6,6 +6,8 @@
 // planes.  Each ray first finds the primitives it can hit at all (liveness pre-pass over
 // a BVH of the leaves), then runs the reference's traversal, skipping subtrees with no
 // live primitive left.
+#include <atomic>
+
 #include "pixel.cuh"
 
 namespace csgrt {
@@ -75,17 +77,22 @@ template <int SD, bool ROLLED>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
     const size_t smem = pix::smem_bytes(SD, p.view.scene.live_words, kThreads, kLocalStacks);
-    // Above the default 48 KiB per block the kernel needs the opt-in; set it once for the
-    // largest layout any scene can ask for (kLiveWordsMax live words).
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads, kLocalStacks));
+    // Above the default 48 KiB per block the kernel needs the opt-in; set it once per device
+    // for the largest layout any scene can ask for (kLiveWordsMax live words), with the
+    // carveout preference.
+    static std::atomic<unsigned long long> attr_set{0};  // bit d: done on device d
+    int device = 0;
+    cudaError_t e = cudaGetDevice(&device);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = device < 64 ? 1ull << device : 0ull;
+    if (!(attr_set.load(std::memory_order_acquire) & bit) || !bit) {
+        e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads, kLocalStacks));
         if (e == cudaSuccess && CSG_TILED_CARVEOUT >= 0)
             e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      CSG_TILED_CARVEOUT);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        attr_set.fetch_or(bit, std::memory_order_release);
     }
     const dim3 grid((p.view.w + kTileW - 1) / kTileW, (p.view.h + kTileH - 1) / kTileH);
     render_tiled<SD, ROLLED><<<grid, kThreads, smem, stream>>>(p);
