@@ -29,7 +29,7 @@ LIB_PATH = PKG_DIR / "_build" / "libcsgrt.so"
 CSG_OK, CSG_E_PARSE, CSG_E_RANGE, CSG_E_COUNT, CSG_E_CUDA = 0, 1, 2, 3, 4
 CSG_E_BUDGET, CSG_E_TIMEOUT, CSG_E_DEPTH, CSG_E_ARG, CSG_E_CAPACITY = 5, 6, 7, 8, 9
 
-# Every symbol include/csgrt.h (and include/csgrt_batch.h) declares.
+# Every function include/csgrt.h declares.
 EXPORTED = [
     "csg_abi_version", "csg_status_string",
     "csg_tree_parse", "csg_scene_create", "csg_scene_destroy", "csg_scene_get_info", "csg_scene_export_reference_layout",
