@@ -1,4 +1,5 @@
-// The view-table kernel (views.hpp) and csg_render_views_noalloc, the batched persistent
+// The view-table launcher (views.hpp; the default block shape is instantiated here, the
+// kernel lives in views_kernel.cuh) and csg_render_views_noalloc, the batched persistent
 // render for callers that must not allocate device memory.
 //
 // Some callers cannot allocate at render time.  A server running at its device-memory

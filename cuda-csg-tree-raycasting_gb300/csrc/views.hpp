@@ -1,7 +1,8 @@
-// Launch interface of the view-table kernel (noalloc.cu): many views of many scenes in one
-// persistent launch whose work items are found by a binary search of a per-view tile
-// prefix, so its tables are O(views).  Used by csg_render_views_noalloc (tables in a
-// fixed device array) and by the render server (tables per in-flight batch).
+// Launch interface of the view-table kernel (views_kernel.cuh): many views of many scenes
+// in one persistent launch whose work items are found by a binary search of a per-view
+// tile prefix, so its tables are O(views).  Used by csg_batch (a table per tree-size
+// class), csg_render_views_noalloc (tables in a fixed device array) and the render server
+// (tables per in-flight batch).
 #pragma once
 
 #include <cstdint>
