@@ -142,6 +142,7 @@ def test_batch_block_shapes_equal_per_view_renders(csg, deep):
 
 
 def test_batch_rejects_bad_shapes(csg):
+    import ctypes
     import torch
     torch.cuda.set_device(0)
     sc = csg.Scene("Sphere 0 0 0 FF0000 1")
@@ -150,6 +151,13 @@ def test_batch_rejects_bad_shapes(csg):
     for warps, local in ((3, 0), (1, 0), (16, 0), (2, 1), (8, 1), (4, 2)):
         assert csg.lib().csg_batch_set_shape(b.h, warps, local) == csg.CSG_E_ARG
     assert csg.lib().csg_batch_set_shape(None, 4, 0) == csg.CSG_E_ARG
+    n = b.info()["n_classes"]
+    for k, tw, warps, local in ((-1, 8, 4, 0), (n, 8, 4, 0), (0, 6, 4, 0), (0, 8, 3, 0), (0, 8, 8, 1)):
+        assert csg.lib().csg_batch_set_class(b.h, k, tw, warps, local) == csg.CSG_E_ARG, (k, tw, warps, local)
+    assert csg.lib().csg_batch_set_class(b.h, 0, 16, 2, 0) == csg.CSG_OK
+    assert (b.classes()[0]["warp_tile_w"], b.classes()[0]["warps_per_block"]) == (16, 2)
+    info = csg.csg_batch_class_info()
+    assert csg.lib().csg_batch_get_class(b.h, n, ctypes.byref(info)) == csg.CSG_E_ARG
     b.close()
     sc.close()
 
