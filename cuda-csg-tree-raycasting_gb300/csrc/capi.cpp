@@ -177,6 +177,9 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.n_bvh = static_cast<int32_t>(pk.bvh.size() / 4);
     s->dev.live_words = pk.live_words;
     s->dev.live_shift = pk.live_shift;
+    s->dev.fine = pk.fine;
+    s->dev.fine_words = pk.fine_words;
+    s->dev.fine_shift = pk.fine_shift;
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
     s->dev.rolled = csgrt::use_rolled(s->tree) ? 1 : 0;
     s->status = reinterpret_cast<unsigned long long*>(base + off_status);

@@ -91,16 +91,17 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
 
 // One pixel.  Must be called by all 32 lanes of a warp (the pre-pass walks the BVH
 // warp-cooperatively); lanes with inside == false only follow the walk.
-template <int SD, bool ROLLED, class Stacks>
+// FINE: the scene's fine live mask (single-view renders of large trees) instead of its own.
+template <int SD, bool ROLLED, bool FINE = false, class Stacks>
 __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long long* status, uint32_t iter_cap,
                                              int x, int y, bool inside, Stacks& st, const BlockSmem& bs,
                                              const uint16_t* tab)
 {
-    dev::LiveMask lm;
+    typename std::conditional<FINE, dev::LiveMaskFine, dev::LiveMask>::type lm;
     lm.w = bs.live + threadIdx.x;
     lm.nt = bs.nt;
-    lm.shift = p.scene.live_shift;
-    lm.words = p.scene.live_words;
+    lm.shift = FINE ? p.scene.fine_shift : p.scene.live_shift;
+    lm.words = FINE ? p.scene.fine_words : p.scene.live_words;
     lm.sum = 0;
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h);
     dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);

@@ -55,7 +55,8 @@ constexpr bool kLocalStacks = CSG_TILED_LOCAL_STACKS != 0;
 #define CSG_TILED_CARVEOUT 80
 #endif
 
-template <int SD, bool ROLLED>
+// FINE: the scene's fine live mask (scenes with scene.fine set; rolled variants only).
+template <int SD, bool ROLLED, bool FINE>
 __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG_UNROLLED_MIN_BLOCKS)
     render_tiled(const RenderParams p)
 {
@@ -65,18 +66,21 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     typename std::conditional<kLocalStacks, dev::LocalStacks<SD>, dev::SmemStacks<SD>>::type st;
     if constexpr (kLocalStacks) pix::init_stacks(st);
     else st = pix::block_stacks<SD, kThreads>(smem_raw);
-    const pix::BlockSmem bs = pix::block_smem<SD, kThreads, kLocalStacks>(smem_raw, p.view.scene.live_words);
+    const pix::BlockSmem bs =
+        pix::block_smem<SD, kThreads, kLocalStacks>(smem_raw, FINE ? p.view.scene.fine_words : p.view.scene.live_words);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int x = blockIdx.x * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
     const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
-    pix::render_pixel<SD, ROLLED>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st, bs, tab);
+    pix::render_pixel<SD, ROLLED, FINE>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st, bs,
+                                        tab);
 }
 
-template <int SD, bool ROLLED>
+template <int SD, bool ROLLED, bool FINE>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
-    const size_t smem = pix::smem_bytes(SD, p.view.scene.live_words, kThreads, kLocalStacks);
+    const int words = FINE ? p.view.scene.fine_words : p.view.scene.live_words;
+    const size_t smem = pix::smem_bytes(SD, words, kThreads, kLocalStacks);
     // Above the default 48 KiB per block the kernel needs the opt-in; set it once per device
     // for the largest layout any scene can ask for (kLiveWordsMax live words), with the
     // carveout preference.
@@ -86,23 +90,24 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
     if (e != cudaSuccess) return e;
     const unsigned long long bit = device < 64 ? 1ull << device : 0ull;
     if (!(attr_set.load(std::memory_order_acquire) & bit) || !bit) {
-        e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)pix::smem_bytes(SD, kLiveWordsMax, kThreads, kLocalStacks));
+        e = cudaFuncSetAttribute(render_tiled<SD, ROLLED, FINE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)pix::smem_bytes(SD, FINE ? kFineWordsMax : kLiveWordsMax, kThreads, kLocalStacks));
         if (e == cudaSuccess && CSG_TILED_CARVEOUT >= 0)
-            e = cudaFuncSetAttribute(render_tiled<SD, ROLLED>, cudaFuncAttributePreferredSharedMemoryCarveout,
+            e = cudaFuncSetAttribute(render_tiled<SD, ROLLED, FINE>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      CSG_TILED_CARVEOUT);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit, std::memory_order_release);
     }
     const dim3 grid((p.view.w + kTileW - 1) / kTileW, (p.view.h + kTileH - 1) / kTileH);
-    render_tiled<SD, ROLLED><<<grid, kThreads, smem, stream>>>(p);
+    render_tiled<SD, ROLLED, FINE><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 
 template <int SD>
 cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
 {
-    return p.view.scene.rolled ? launch_variant<SD, true>(p, stream) : launch_variant<SD, false>(p, stream);
+    if (!p.view.scene.rolled) return launch_variant<SD, false, false>(p, stream);
+    return p.view.scene.fine ? launch_variant<SD, true, true>(p, stream) : launch_variant<SD, true, false>(p, stream);
 }
 
 __global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fmul_rn(fov, 0.5f)); }

@@ -491,6 +491,7 @@ struct BvhBuilder {
 void pack_scene(const HostTree& t, PackedScene& out)
 {
     const size_t n = t.nodes.size(), np = t.prims.size();
+    const bool rolled = use_rolled(t);
     // Device node numbering: the operators first, in preorder (the root, node 0 of the
     // reference, stays 0), then the leaves.  Only operators have kids records, so those are
     // dense and a cache line holds only records the traversal reads.
@@ -534,6 +535,11 @@ void pack_scene(const HostTree& t, PackedScene& out)
     while (((static_cast<int64_t>(np) + (1 << shift) - 1) >> shift) > 32 * kLiveWordsMax) ++shift;
     out.live_shift = shift;
     out.live_words = static_cast<int32_t>((((np + (1u << shift) - 1) >> shift) + 31) / 32);
+    int32_t fshift = 0;
+    while (((static_cast<int64_t>(np) + (1 << fshift) - 1) >> fshift) > 32 * kFineWordsMax) ++fshift;
+    out.fine_shift = fshift;
+    out.fine_words = static_cast<int32_t>((((np + (1u << fshift) - 1) >> fshift) + 31) / 32);
+    out.fine = (rolled && shift > 0 && fshift == 0 && out.fine_words <= CSG_FINE_WORDS_USE) ? 1 : 0;
     // BVH over the leaves' reference boxes (primitive order -> node order)
     out.bvh.clear();
     if (np >= 2) {

@@ -83,6 +83,18 @@ constexpr int kKidsPerNode = 5;
 #endif
 constexpr int kLiveWordsMax = CSG_LIVE_WORDS_MAX;
 static_assert(kLiveWordsMax >= 1 && kLiveWordsMax <= 64, "live-mask words");
+// Fine live mask of single-view renders (the render_tiled variants for rolled scenes):
+// one bit per leaf, up to kFineWordsMax words, used for a scene whose own mask groups
+// leaves (more than 32 * kLiveWordsMax of them) when the fine mask needs at most
+// CSG_FINE_WORDS_USE words.  Measured on the batched workload's 35 trees of 1,025-2,015
+// leaves, as single views: one bit per leaf up to 1,824 leaves (57 words) is faster for
+// most (up to 20%), the larger ones run up to 13% slower (fewer resident blocks), and a
+// tree of ~3,600 leaves with two leaves per bit instead of four ran 8% slower, so only
+// one bit per leaf is used.  0 disables it.
+constexpr int kFineWordsMax = 64;
+#ifndef CSG_FINE_WORDS_USE
+#define CSG_FINE_WORDS_USE 57
+#endif
 
 struct DeviceScene {
     const int4* topo = nullptr;
@@ -97,6 +109,9 @@ struct DeviceScene {
     int32_t n_bvh = 0;        // BVH nodes (0: a single primitive, no BVH)
     int32_t live_words = 0;   // words of the per-ray live mask
     int32_t live_shift = 0;   // log2 of the leaves per live bit
+    int32_t fine = 0;         // single-view renders use the fine mask below
+    int32_t fine_words = 0;   // its words (at most kFineWordsMax)
+    int32_t fine_shift = 0;   // its log2 of the leaves per bit
     int32_t prepass = 0;      // run the liveness pre-pass (scenes with enough leaves)
     int32_t rolled = 0;       // kernel variant: GoTo's tests in a rolled loop (see trace.cuh)
 };
@@ -110,6 +125,9 @@ struct PackedScene {
     std::vector<float4> bvh;
     int32_t live_words = 0;
     int32_t live_shift = 0;
+    int32_t fine = 0;
+    int32_t fine_words = 0;
+    int32_t fine_shift = 0;
 };
 void pack_scene(const HostTree& tree, PackedScene& out);
 

@@ -525,10 +525,13 @@ struct LocalStacks {
 // output, so skipping such a subtree changes nothing.  Bits are cleared when a leaf test
 // returns Miss and when an operator child's box culls (its leaves' boxes are nested in
 // it, so they cull too).  The mask lives in shared memory, word k of a lane at
-// w[k * nt]; `sum` has bit k set while word k is non-zero.
+// w[k * nt]; `sum` has bit k set while word k is non-zero (SumT: 32 bits for masks of up
+// to 32 words, 64 bits for up to 64).
 using live_sum_t = std::conditional<(kLiveWordsMax > 32), unsigned long long, uint32_t>::type;
 
-struct LiveMask {
+template <typename SumT>
+struct LiveMaskT {
+    using live_sum_t = SumT;
     uint32_t* w;
     int nt;
     int shift;
@@ -593,6 +596,10 @@ struct LiveMask {
         }
     }
 };
+// The scene's own mask (at most kLiveWordsMax words), and the fine mask of single-view
+// renders of large trees (at most kFineWordsMax words, one bit per leaf up to 2,048 leaves).
+using LiveMask = LiveMaskT<live_sum_t>;
+using LiveMaskFine = LiveMaskT<unsigned long long>;
 
 constexpr int kWarpStack = 64;
 
@@ -624,8 +631,8 @@ __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* 
 // (box_may_pass_at_zero) and whose primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
 // active == false only follow.  If the walk would overflow the warp's stack, every lane
 // falls back to an all-live mask (the traversal then decides everything itself).
-template <bool ROLLED>
-__device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LiveMask& lm,
+template <bool ROLLED, class LM>
+__device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
                                              int* wstack)
 {
     const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
@@ -702,8 +709,9 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 //
 // With boxed == false the same code serves GoTo landing on a leaf (the root is a leaf, or a
 // loop re-enters a leaf child), where the reference calls hitPrimitive with no box test.
+template <class LM>
 __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restrict__ geo, float4 lo, float4 hi,
-                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LiveMask& lm,
+                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LM& lm,
                                            bool boxed = true)
 {
     if (!lm.any(leaf_lo, leaf_hi)) {
@@ -794,9 +802,9 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
 // in one rolled loop, so the primitive tests exist once in the code; the unrolled form
 // overlaps the two children's tests and is faster when the code stays small (scenes
 // without cylinders).
-template <int SD, bool ROLLED, class Stacks>
+template <int SD, bool ROLLED, class Stacks, class LM>
 __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Stacks& st,
-                                            const uint16_t* tab, LiveMask& lm)
+                                            const uint16_t* tab, LM& lm)
 {
     const int4* __restrict__ topo = sc.topo;
     const float4* __restrict__ kids = sc.kids;
@@ -936,9 +944,9 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
 
 // Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
 // stopped at iter_cap; *capped is then set).
-template <int SD, bool ROLLED, class Stacks>
+template <int SD, bool ROLLED, class Stacks, class LM>
 __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, Stacks& st,
-                                            const uint16_t* tab, LiveMask& lm, uint32_t iter_cap, bool* capped)
+                                            const uint16_t* tab, LM& lm, uint32_t iter_cap, bool* capped)
 {
     Tracer T;
     T.ray = ray;
