@@ -248,6 +248,10 @@ int csg_scene_get_info(const csg_scene* s, csg_scene_info* info)
     info->op_depth = s->dev.op_depth;
     info->stack_class = s->dev.stack_class;
     info->device_bytes = s->bytes;
+    info->rolled = s->dev.rolled;
+    info->live_words = s->dev.live_words;
+    info->live_shift = s->dev.live_shift;
+    info->fine_words = s->dev.fine ? s->dev.fine_words : 0;
     return CSG_OK;
 }
 

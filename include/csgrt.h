@@ -60,6 +60,10 @@ typedef struct csg_scene_info {
     int32_t op_depth;     /* most operator nodes on any root-to-leaf path */
     int32_t stack_class;  /* per-ray stack capacity the kernels use for this scene */
     uint64_t device_bytes;/* device memory held by the scene */
+    int32_t rolled;       /* kernel variant: GoTo's child tests in a rolled loop */
+    int32_t live_words;   /* words of the per-ray live-leaf mask (batched renders) */
+    int32_t live_shift;   /* log2 of the leaves per mask bit */
+    int32_t fine_words;   /* words of the one-bit-per-leaf mask of single-view renders, 0 if unused */
 } csg_scene_info;
 
 /* Optional per-pixel planes.  Any pointer may be NULL.  Row-major, w*h entries, row 0 is
