@@ -42,7 +42,7 @@ EXPORTED = [
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
     "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex", "csg_batch_set_shape", "csg_batch_get_class",
-    "csg_render_host", "csg_batch_set_class",
+    "csg_render_host", "csg_batch_set_class", "csg_set_iteration_cap",
 ]
 
 _vp = ctypes.c_void_p
@@ -159,6 +159,7 @@ def lib() -> ctypes.CDLL:
     L.csg_render_f4.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
     L.csg_render_planes.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, ctypes.POINTER(csg_planes), _vp]
     L.csg_render_host.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
+    L.csg_set_iteration_cap.argtypes = [ctypes.c_uint32]
     L.csg_scene_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_device_tan_half_fov.argtypes = [_f, ctypes.POINTER(_f)]
     L.csg_probe_fp32_peak.argtypes = [ctypes.POINTER(_f), ctypes.POINTER(_f)]

@@ -301,7 +301,7 @@ int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out)
         l.counter = c.d_counter;
         l.n_views = (int32_t)n;
         l.live_words = c.live_words;
-        l.iter_cap = csgrt::kIterCap;
+        l.iter_cap = csgrt::iteration_cap();
         l.remaining = nullptr;
         l.done_flags = nullptr;
         l.epoch = 0;

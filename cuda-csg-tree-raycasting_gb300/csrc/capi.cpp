@@ -396,6 +396,12 @@ int csg_render_host(const csg_scene* s, const csg_camera* cam, const float light
     return rc;
 }
 
+int csg_set_iteration_cap(uint32_t cap)
+{
+    csgrt::set_iteration_cap(cap ? cap : csgrt::kIterCap);
+    return CSG_OK;
+}
+
 int csg_device_tan_half_fov(float fov, float* out)
 {
     if (!out) return CSG_E_ARG;

@@ -193,7 +193,7 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
     l.n_items = static_cast<int32_t>(total);
     l.tw_log2 = tile_log2(tw);
     l.live_words = live;
-    l.iter_cap = kIterCap;
+    l.iter_cap = iteration_cap();
     l.remaining = nullptr;
     l.done_flags = nullptr;
     l.epoch = 0;

@@ -114,6 +114,13 @@ __global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fmul_
 
 }  // namespace
 
+namespace {
+std::atomic<uint32_t> g_iter_cap{kIterCap};
+}  // namespace
+
+uint32_t iteration_cap() { return g_iter_cap.load(std::memory_order_relaxed); }
+void set_iteration_cap(uint32_t cap) { g_iter_cap.store(cap, std::memory_order_relaxed); }
+
 cudaError_t device_tan_half_fov(float fov, float* host_out)
 {
     float* d = nullptr;
@@ -140,7 +147,7 @@ cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const flo
     p.view.h = h;
     p.view.out = out;
     p.status = status;
-    p.iter_cap = kIterCap;
+    p.iter_cap = iteration_cap();
     switch (scene.stack_class) {
         case 4: return launch_sd<4>(p, stream);
         case 8: return launch_sd<8>(p, stream);

@@ -34,8 +34,12 @@ struct ViewParams {
 // never reached by a well-formed tree and only stops a runaway ray on a shared GPU.
 constexpr uint32_t kIterCap = 1u << 20;
 
+// The cap the next launches use (kIterCap unless csg_set_iteration_cap changed it).
+uint32_t iteration_cap();
+void set_iteration_cap(uint32_t cap);
+
 // Fused RaycastKernel + LightningKernel for one view of one scene.  `status` is a device
-// counter incremented once per ray that stopped at kIterCap.
+// counter incremented once per ray that stopped at the iteration cap.
 cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const float light[3],
                           int32_t w, int32_t h, const Planes& out,
                           unsigned long long* status, cudaStream_t stream);

@@ -448,7 +448,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
                 vl.n_items = (int32_t)total;
                 vl.tw_log2 = csgrt::tile_log2(tw);
                 vl.live_words = live;
-                vl.iter_cap = csgrt::kIterCap;
+                vl.iter_cap = csgrt::iteration_cap();
                 vl.remaining = S.d_remaining;
                 vl.done_flags = S.d_flags;
                 vl.epoch = L->epoch;

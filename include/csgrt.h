@@ -145,6 +145,12 @@ int csg_render_host(const csg_scene* scene, const csg_camera* cam, const float l
 /* Synchronises `stream` and reports how many rays of the renders issued since the last
  * call stopped at the traversal iteration cap (CSG_E_TIMEOUT if any, else CSG_OK). */
 int csg_scene_check(const csg_scene* scene, void* stream, uint64_t* n_capped);
+/* No counterpart in the reference (whose traversal loop has no bound).  Sets the per-ray
+ * cap on traversal iterations of the renders enqueued after the call (0 restores the
+ * default, 2^20, which no well-formed tree reaches); a ray that reaches it is written as a
+ * miss and counted (csg_scene_check, csg_batch_check).  A batch keeps the cap in force
+ * when it was created.  Process-wide. */
+int csg_set_iteration_cap(uint32_t cap);
 
 /* ---- batches: many views of many scenes in one persistent launch --------------------
  * No counterpart in the reference, which renders one view per Raycast call; the per-view
