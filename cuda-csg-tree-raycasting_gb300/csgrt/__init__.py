@@ -112,7 +112,7 @@ class csg_server_stats(ctypes.Structure):
     _fields_ = [("budget", ctypes.c_uint64), ("scene_bytes", ctypes.c_uint64), ("output_bytes", ctypes.c_uint64),
                 ("peak_bytes", ctypes.c_uint64), ("requests_done", ctypes.c_int64), ("batches", ctypes.c_int64),
                 ("evictions", ctypes.c_int64), ("rejected", ctypes.c_int64), ("scenes", _i32),
-                ("resident_scenes", _i32), ("slots_busy", _i32), ("pending", _i32)]
+                ("resident_scenes", _i32), ("slots_busy", _i32), ("pending", _i32), ("capped_rays", ctypes.c_uint64)]
 
 
 _LIB = None

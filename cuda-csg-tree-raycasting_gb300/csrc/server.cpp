@@ -175,6 +175,7 @@ struct csg_server {
     std::list<Launch*> tracked;       // launches in flight, watched by the poller
     std::vector<cudaEvent_t> events;  // completion events not in use
     cudaStream_t alone = nullptr;     // stream of the unbatched launches
+    unsigned long long* d_capped = nullptr;  // rays of any request stopped at the iteration cap
     size_t table_head = 0;            // bytes before a slot's view records
     cudaMemPool_t pool = nullptr;
     uint64_t scene_bytes = 0, output_bytes = 0, peak = 0, use_clock = 0;
@@ -413,7 +414,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
             Req* q = batch[0];
             csgrt::Camera cam;
             std::memcpy(cam.v, &q->r.cam, sizeof(cam.v));
-            e = csgrt::launch_render(sc[0]->dev, cam, q->r.light_dir, q->r.w, q->r.h, q->planes, sc[0]->status, st);
+            e = csgrt::launch_render(sc[0]->dev, cam, q->r.light_dir, q->r.w, q->r.h, q->planes, d_capped, st);
         } else {
             // view table in arrival order, tile prefix, per-view remaining tiles
             Slot& S = slots[slot];
@@ -423,7 +424,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
             int64_t total = 0;
             for (size_t k = 0; k < batch.size(); ++k) {
                 const Req* q = batch[k];
-                csgrt::make_view_record(sc[k]->dev, sc[k]->status, reinterpret_cast<const float*>(&q->r.cam),
+                csgrt::make_view_record(sc[k]->dev, d_capped, reinterpret_cast<const float*>(&q->r.cam),
                                         q->r.light_dir, q->r.w, q->r.h, q->planes, tw, S.h_views[k]);
                 S.h_views[k].host_out = q->host_direct ? 1 : 0;
                 const int64_t tiles = csgrt::view_tiles(q->r.w, q->r.h, tw);
@@ -598,6 +599,8 @@ int csg_server_create(const csg_server_config* cfg_in, csg_server** out)
         e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
     }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->alone, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_capped, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(s->d_capped, 0, sizeof(unsigned long long));
     const size_t nv = (size_t)cfg.max_batch_views;
     // [counter | pad to 16][prefix: nv + 1][remaining: nv][pad to 16][views], the same
     // layout staged on the host, so that one copy (its length set by the views in the
@@ -672,6 +675,7 @@ int csg_server_destroy(csg_server* s)
     }
     if (s->alone) cudaStreamDestroy(s->alone);
     for (cudaEvent_t ev : s->events) cudaEventDestroy(ev);
+    if (s->d_capped) cudaFree(s->d_capped);
     if (s->pool) cudaMemPoolDestroy(s->pool);
     delete s;
     return CSG_OK;
@@ -875,6 +879,11 @@ int csg_server_replay(csg_server* s, const csg_request* reqs, const double* arri
 int csg_server_stats_get(csg_server* s, csg_server_stats* o)
 {
     if (!s || !o) return CSG_E_ARG;
+    // rays stopped at the iteration cap so far (a count that only grows; launches still in
+    // flight may add to it)
+    unsigned long long capped = 0;
+    if (cudaMemcpy(&capped, s->d_capped, sizeof(capped), cudaMemcpyDeviceToHost) != cudaSuccess) return CSG_E_CUDA;
+    o->capped_rays = capped;
     std::lock_guard<std::mutex> lk(s->mu);
     o->budget = s->cfg.hbm_budget;
     o->scene_bytes = s->scene_bytes;

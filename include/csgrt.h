@@ -292,6 +292,7 @@ typedef struct csg_server_stats {
     uint64_t budget, scene_bytes, output_bytes, peak_bytes;
     int64_t requests_done, batches, evictions, rejected;
     int32_t scenes, resident_scenes, slots_busy, pending;
+    uint64_t capped_rays;  /* rays of all requests stopped at the traversal iteration cap */
 } csg_server_stats;
 
 int csg_server_create(const csg_server_config* cfg, csg_server** out);

@@ -55,3 +55,34 @@ def test_iteration_cap_runs_out_and_is_reported(csg):
             assert torch.equal(again["rgba8"], ref["rgba8"]) and torch.equal(again["prim"], ref["prim"])
     finally:
         lib.csg_set_iteration_cap(0)
+
+
+def test_server_counts_capped_rays(csg):
+    """Served requests (batched and one launch each) whose rays reach the cap still complete;
+    the server's statistics count the capped rays."""
+    from csgrt import scenes
+    text = scenes.config_scene_text(2, 0)
+    view = scenes.config_views(2, 0)[0]
+    cam = csg.Camera.from_floats(view.camera)
+    lib = csg.lib()
+    srv = csg.Server(hbm_budget=2 << 30, slots=2, max_batch_views=16)
+    try:
+        sid = srv.add_scene(text)
+        res, _, _ = srv.replay([csg.Server.request(sid, cam, view.light, 128, 96, alone=a) for a in (False, True)],
+                               [0.0, 0.0])
+        assert all(r.status == 0 for r in res)
+        assert srv.stats()["capped_rays"] == 0
+        assert lib.csg_set_iteration_cap(4) == csg.CSG_OK
+        res, _, _ = srv.replay([csg.Server.request(sid, cam, view.light, 128, 96, alone=a) for a in (False, True)],
+                               [0.0, 0.0])
+        assert all(r.status == 0 for r in res)
+        capped = srv.stats()["capped_rays"]
+        assert capped > 0
+        lib.csg_set_iteration_cap(0)
+        res, _, _ = srv.replay([csg.Server.request(sid, cam, view.light, 128, 96, alone=a) for a in (False, True)],
+                               [0.0, 0.0])
+        assert all(r.status == 0 for r in res)
+        assert srv.stats()["capped_rays"] == capped  # no new ones
+    finally:
+        lib.csg_set_iteration_cap(0)
+        srv.close()
