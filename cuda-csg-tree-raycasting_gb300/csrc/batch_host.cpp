@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "csgrt.h"
+#include "planes.hpp"
 #include "scene_handle.hpp"
 #include "views.hpp"
 
@@ -114,45 +115,6 @@ int set_shape(csg_batch* b, BatchClass& c, csgrt::ViewsShape s)
     return CSG_OK;
 }
 
-// The address the kernel writes an output plane through: device (or managed) memory as
-// it is, page-locked host memory through its mapped device address.  Pageable host
-// memory cannot be written by a kernel and is refused.
-int plane_address(void* p, void** dev)
-{
-    *dev = nullptr;
-    if (!p) return CSG_OK;
-    cudaPointerAttributes a{};
-    const cudaError_t e = cudaPointerGetAttributes(&a, p);
-    cudaGetLastError();  // an unregistered pointer may leave an error behind on older runtimes
-    if (e != cudaSuccess) return CSG_E_ARG;
-    if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) {
-        *dev = p;
-        return CSG_OK;
-    }
-    if (a.type == cudaMemoryTypeHost && a.devicePointer) {
-        *dev = a.devicePointer;
-        return CSG_OK;
-    }
-    return CSG_E_ARG;
-}
-
-int device_planes(csg_planes& out)
-{
-    void* d = nullptr;
-    int rc = CSG_OK;
-    if ((rc = plane_address(out.rgba8, &d)) != CSG_OK) return rc;
-    out.rgba8 = static_cast<uint32_t*>(d);
-    if ((rc = plane_address(out.rgba32f, &d)) != CSG_OK) return rc;
-    out.rgba32f = static_cast<float*>(d);
-    if ((rc = plane_address(out.t, &d)) != CSG_OK) return rc;
-    out.t = static_cast<float*>(d);
-    if ((rc = plane_address(out.prim, &d)) != CSG_OK) return rc;
-    out.prim = static_cast<int32_t*>(d);
-    if ((rc = plane_address(out.normal, &d)) != CSG_OK) return rc;
-    out.normal = static_cast<float*>(d);
-    return CSG_OK;
-}
-
 // One class's work on `st`: counter reset and the persistent launch.
 cudaError_t enqueue_class(const csg_batch* b, const BatchClass& c, cudaStream_t st)
 {
@@ -232,7 +194,7 @@ int csg_batch_create(const csg_view* views, int32_t n_views, csg_batch** out)
     cudaGetDevice(&b->device);
     b->src.assign(views, views + n_views);
     for (csg_view& v : b->src) {
-        const int rc = device_planes(v.out);
+        const int rc = csgrt::device_planes(v.out);
         if (rc != CSG_OK) {
             delete b;
             return rc;

@@ -34,6 +34,7 @@
 
 #include "csgrt.h"
 #include "pixel.cuh"
+#include "planes.hpp"
 #include "scene_handle.hpp"
 #include "views_kernel.cuh"
 
@@ -138,6 +139,8 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
         const csg_view& v = views[i];
         if (!v.scene || v.w <= 0 || v.h <= 0) return CSG_E_ARG;
         if (v.out.rgba32f && (reinterpret_cast<uintptr_t>(v.out.rgba32f) & 15u)) return CSG_E_ARG;
+        csg_planes dp = v.out;  // checked before anything is enqueued
+        if (device_planes(dp) != CSG_OK) return CSG_E_ARG;
         sd = std::max(sd, v.scene->dev.stack_class);
         live = std::max(live, v.scene->dev.live_words);
         rolled = rolled || v.scene->dev.rolled;
@@ -171,8 +174,9 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
         const int32_t n = std::min<int32_t>(kChunk, n_views - k0);
         for (int32_t j = 0; j < n; ++j) {
             const csg_view& v = views[order[k0 + j]];
-            const Planes out{v.out.rgba8, reinterpret_cast<float4*>(v.out.rgba32f), v.out.t, v.out.prim,
-                             v.out.normal};
+            csg_planes dp = v.out;
+            device_planes(dp);  // checked above
+            const Planes out{dp.rgba8, reinterpret_cast<float4*>(dp.rgba32f), dp.t, dp.prim, dp.normal};
             make_view_record(v.scene->dev, v.scene->status, reinterpret_cast<const float*>(&v.cam), v.light_dir,
                              v.w, v.h, out, tw, c.rec[j]);
             c.prefix[j] = prefix[k0 + j];

@@ -234,7 +234,9 @@ int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
  * image.  For callers that cannot allocate at render time -- a server at its
  * device-memory budget, a frame loop that cannot take the device-wide synchronisation of
  * cudaFree.  warp_tile_w is 4, 8, 16 or 32 (0: 8).  More than CSG_NOALLOC_MAX_VIEWS views
- * gives CSG_E_CAPACITY, before anything is enqueued.  Asynchronous on `stream`; capped
+ * gives CSG_E_CAPACITY, and a view with pageable host planes CSG_E_ARG, before anything
+ * is enqueued (planes may be device or page-locked host memory, as for csg_batch_create).
+ * Asynchronous on `stream`; capped
  * rays are counted per scene (csg_scene_check).  The first call on a device does set-up
  * (looks up the array's address, sets kernel attributes): make it before any stream
  * capture on that device.  All calls on a device share the one array, so calls whose

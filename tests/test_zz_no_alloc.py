@@ -1,7 +1,8 @@
 """csg_render_views_noalloc (the batched render whose scratch is a fixed device array)
 writes, on two calls in a row, exactly the bytes the allocating entry points write --
-csg_render_planes per view and csg_batch_render for the whole set -- and rejects view
-counts beyond its fixed capacity before enqueuing anything.  Collected last on purpose:
+csg_render_planes per view and csg_batch_render for the whole set -- writes page-locked
+host planes directly, and rejects view counts beyond its fixed capacity and pageable host
+planes before enqueuing anything.  Collected last on purpose:
 it must pass after every other test has used the device, as well as alone."""
 from __future__ import annotations
 
@@ -95,6 +96,17 @@ def test_noalloc_matches_allocating_entry_points_twice_in_a_row(csg):
                 assert torch.equal(r[k], o[k]), (call, i, k)
     for sc in objs:
         assert sc.check() == 0
+
+    # page-locked host planes are written by the kernel; pageable ones are refused up front
+    sc, cam, light, w, h = specs[0]
+    pinned = torch.zeros(w * h, dtype=torch.int32, pin_memory=True)
+    harr = _view_array(csg, [(sc, cam, light, w, h, {"rgba8": pinned.data_ptr()})])
+    assert csg.lib().csg_render_views_noalloc(harr, 1, 8, stream) == csg.CSG_OK
+    torch.cuda.synchronize()
+    assert torch.equal(pinned, ref[0]["rgba8"].cpu())
+    pageable = np.zeros(w * h, dtype=np.int32)
+    parr = _view_array(csg, [(sc, cam, light, w, h, {"rgba8": pageable.ctypes.data})])
+    assert csg.lib().csg_render_views_noalloc(parr, 1, 8, stream) == csg.CSG_E_ARG
     batch.close()
     for sc in objs:
         sc.close()
