@@ -95,7 +95,7 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
 template <int SD, bool ROLLED, bool FINE = false, class Stacks>
 __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long long* status, uint32_t iter_cap,
                                              int x, int y, bool inside, Stacks& st, const BlockSmem& bs,
-                                             const uint16_t* tab)
+                                             const uint16_t* tab, dev::RayFrame frame)
 {
     typename std::conditional<FINE, dev::LiveMaskFine, dev::LiveMask>::type lm;
     lm.w = bs.live + threadIdx.x;
@@ -103,7 +103,7 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     lm.shift = FINE ? p.scene.fine_shift : p.scene.live_shift;
     lm.words = FINE ? p.scene.fine_words : p.scene.live_words;
     lm.sum = 0;
-    const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h);
+    const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h, frame);
     dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
     bool capped = false;

@@ -62,7 +62,9 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint16_t tab[27];
+    __shared__ dev::RayFrame frame;  // the view's ray-generation factors, computed once per block
     pix::load_table(tab);
+    if (threadIdx.x == 32) frame = dev::ray_frame(p.view.cam.v, (float)p.view.w, (float)p.view.h);
     typename std::conditional<kLocalStacks, dev::LocalStacks<SD>, dev::SmemStacks<SD>>::type st;
     if constexpr (kLocalStacks) pix::init_stacks(st);
     else st = pix::block_stacks<SD, kThreads>(smem_raw);
@@ -73,7 +75,7 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
     pix::render_pixel<SD, ROLLED, FINE>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st, bs,
-                                        tab);
+                                        tab, frame);
 }
 
 template <int SD, bool ROLLED, bool FINE>

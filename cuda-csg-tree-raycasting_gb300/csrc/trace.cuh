@@ -125,14 +125,25 @@ __device__ __forceinline__ void ray_finish(Ray& r)
     r.exact = sub(r.d.x) || sub(r.d.y) || sub(r.d.z);
 }
 
+// The per-view factors of ray generation: tan(fov / 2) and width / height, as the
+// reference computes them for every ray (the same bits whoever computes them).
+struct RayFrame {
+    float thf, aspect;
+};
+__device__ __forceinline__ RayFrame ray_frame(const float* cam, float width, float height)
+{
+    return RayFrame{tanf(__fmul_rn(cam[5], 0.5f)), __fdiv_rn(width, height)};
+}
+
 // RaycastKernel ray generation (RaycastingKernels.cu:11-27) + the Ray constructor's
 // second normalisation (Ray.cuh:12-18).  width/height are floats, as in the reference.
-__device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float width, float height)
+__device__ __forceinline__ Ray primary_ray(const float* cam, int x, int y, float width, float height,
+                                           RayFrame f)
 {
     const float u = __fdiv_rn(__fadd_rn((float)x, 0.5f), __fsub_rn(width, 1.0f));
     const float v = __fdiv_rn(__fadd_rn((float)y, 0.5f), __fsub_rn(height, 1.0f));
-    const float thf = tanf(__fmul_rn(cam[5], 0.5f));
-    const float nx = __fmul_rn(__fmul_rn(__fmaf_rn(2.0f, u, -1.0f), __fdiv_rn(width, height)), thf);
+    const float thf = f.thf;
+    const float nx = __fmul_rn(__fmul_rn(__fmaf_rn(2.0f, u, -1.0f), f.aspect), thf);
     const float ny = __fmul_rn(__fmaf_rn(-2.0f, v, 1.0f), thf);
     V3 d;
     d.x = __fadd_rn(__fmaf_rn(cam[9], nx, __fmul_rn(cam[12], ny)), cam[6]);

@@ -59,7 +59,8 @@ __global__ void __launch_bounds__(NT, CSG_VIEWS_MIN_BLOCKS * pix::kThreads / NT)
         const int tx = tile % v.tiles_x, ty = tile / v.tiles_x;
         const int x = tx * tw + ox, y = ty * th + oy;
         const bool inside = x < v.view.w && y < v.view.h;
-        pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab);
+        pix::render_pixel<SD, ROLLED>(v.view, v.status, p.iter_cap, x, y, inside, st, bs, tab,
+                                      dev::ray_frame(v.view.cam.v, (float)v.view.w, (float)v.view.h));
         if (p.remaining) {
             if (v.host_out) __threadfence_system();  // this lane's host-mapped plane
             else __threadfence();
