@@ -45,7 +45,7 @@ cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const flo
                           unsigned long long* status, cudaStream_t stream);
 
 // tan(fov / 2) exactly as the kernels' ray generation computes it (device tanf);
-// a diagnostic for checkers that restate the ray generation on the host.
+// a diagnostic for host code that restates the ray generation.
 cudaError_t device_tan_half_fov(float fov, float* host_out);
 
 }  // namespace csgrt
