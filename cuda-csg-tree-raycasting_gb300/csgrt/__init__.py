@@ -42,7 +42,7 @@ EXPORTED = [
     "csg_server_create", "csg_server_destroy", "csg_server_add_scene", "csg_server_preload", "csg_server_submit",
     "csg_server_wait", "csg_server_release", "csg_server_replay", "csg_server_stats_get", "csg_server_clock",
     "csg_image_write", "csg_scene_create_ex", "csg_tree_parse_ex", "csg_batch_set_shape", "csg_batch_get_class",
-    "csg_render_host", "csg_batch_set_class", "csg_set_iteration_cap",
+    "csg_render_host", "csg_batch_set_class", "csg_set_iteration_cap", "csg_tree_plan",
 ]
 
 _vp = ctypes.c_void_p
@@ -160,6 +160,8 @@ def lib() -> ctypes.CDLL:
     L.csg_render_planes.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, ctypes.POINTER(csg_planes), _vp]
     L.csg_render_host.argtypes = [_vp, C, ctypes.POINTER(_f), _i32, _i32, _vp, _vp]
     L.csg_set_iteration_cap.argtypes = [ctypes.c_uint32]
+    L.csg_tree_plan.argtypes = [ctypes.c_char_p, ctypes.c_size_t, _i32, ctypes.POINTER(csg_scene_info),
+                                ctypes.c_char_p, ctypes.c_size_t]
     L.csg_scene_check.argtypes = [_vp, _vp, ctypes.POINTER(ctypes.c_uint64)]
     L.csg_device_tan_half_fov.argtypes = [_f, ctypes.POINTER(_f)]
     L.csg_probe_fp32_peak.argtypes = [ctypes.POINTER(_f), ctypes.POINTER(_f)]
@@ -245,6 +247,19 @@ def parse_tree(text: str | bytes, exact_boxes: bool = False):
     check(lib().csg_tree_parse_ex(data, len(data), flags, nodes.ctypes.data, nn.value, prims.ctypes.data,
                                   npr.value, ctypes.byref(nn), ctypes.byref(npr), ctypes.byref(dep), err, 512))
     return nodes, prims, dep.value
+
+
+def plan_tree(text: str | bytes, exact_boxes: bool = False) -> dict:
+    """csg_tree_plan: what a Scene built from `text` would hold (sizes, kernel variant, live
+    masks), computed on the host alone."""
+    data = text.encode() if isinstance(text, str) else bytes(text)
+    inf = csg_scene_info()
+    err = ctypes.create_string_buffer(512)
+    rc = lib().csg_tree_plan(data, len(data), CSG_SCENE_EXACT_BOXES if exact_boxes else 0, ctypes.byref(inf), err,
+                             512)
+    if rc != CSG_OK:
+        raise CsgError(rc, err.value.decode(errors="replace"))
+    return {k: getattr(inf, k) for k, _ in csg_scene_info._fields_}
 
 
 # ------------------------------------------------------------------------------------

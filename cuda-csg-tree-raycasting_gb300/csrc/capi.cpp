@@ -187,6 +187,34 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     return CSG_OK;
 }
 
+int csg_tree_plan(const char* text, size_t len, int32_t flags, csg_scene_info* info, char* err, size_t errlen)
+{
+    if (!info || (!text && len)) return CSG_E_ARG;
+    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
+    csgrt::HostTree tree;
+    std::string msg;
+    const int rc = csgrt::parse_tree(std::string_view(text ? text : "", len), tree, msg);
+    if (rc != csgrt::kOk) {
+        copy_err(err, errlen, msg);
+        return rc;
+    }
+    if (flags & CSG_SCENE_EXACT_BOXES) csgrt::use_exact_boxes(tree);
+    csgrt::PackedScene pk;
+    csgrt::pack_scene(tree, pk);
+    const size_t n = tree.nodes.size(), np = tree.prims.size();
+    *info = csg_scene_info{};
+    info->n_nodes = static_cast<int32_t>(n);
+    info->n_prims = static_cast<int32_t>(np);
+    info->op_depth = tree.op_depth;
+    info->stack_class = csgrt::stack_class_for_depth(tree.op_depth);
+    info->device_bytes = csgrt::scene_layout(n, np, pk.kids.size(), pk.bvh.size()).total;
+    info->rolled = csgrt::use_rolled(tree) ? 1 : 0;
+    info->live_words = pk.live_words;
+    info->live_shift = pk.live_shift;
+    info->fine_words = pk.fine ? pk.fine_words : 0;
+    return CSG_OK;
+}
+
 int csg_tree_parse(const char* text, size_t len, void* nodes44, int32_t max_nodes, void* prims48,
                    int32_t max_prims, int32_t* n_nodes, int32_t* n_prims, int32_t* op_depth,
                    char* err, size_t errlen)

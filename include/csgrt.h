@@ -92,6 +92,10 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
 /* Frees the scene's device memory (Raycaster::CleanUp, Raycaster.cu:36-44). */
 int csg_scene_destroy(csg_scene* scene);
 int csg_scene_get_info(const csg_scene* scene, csg_scene_info* info);
+/* What csg_scene_create(_ex) would build for this text, computed on the host alone (no
+ * device work): the same fields csg_scene_get_info reports for the created scene.  Parse
+ * errors as csg_scene_create. */
+int csg_tree_plan(const char* text, size_t len, int32_t flags, csg_scene_info* info, char* err, size_t errlen);
 /* CSGTree::Parse alone (host only, no device work): parses and builds the boxes into the
  * reference's own record layouts, 44-byte CSGNode (CSGTree.cuh:15-34) and 48-byte
  * Primitive (Primitives.h:29-40).  Pass NULL arrays to query the counts.  Unused

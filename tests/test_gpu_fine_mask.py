@@ -26,6 +26,7 @@ def test_fine_mask_trees_vs_reference_kernel(csg):
         text = scenes.write_text(scenes.random_tree(seed, 2, 2048, 12))
         with csg.Scene(text) as sc:
             info = sc.info()
+        assert info == csg.plan_tree(text)  # the host-side plan is what the scene holds
         assert info["n_prims"] > 1024 and info["rolled"] == 1 and info["live_shift"] == 1, (seed, info)
         assert (info["fine_words"] > 0) == fine, (seed, info)
         if fine:

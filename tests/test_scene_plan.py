@@ -1,0 +1,61 @@
+"""The scene compiler's host-side decisions (csg_tree_plan, no device work): stack class
+from the operator depth, rolled GoTo for trees with cylinders and more than 8 primitives,
+live-mask words and granularity, the fine mask of single-view renders for rolled trees of
+1,025-1,824 leaves, and the device layout size."""
+from __future__ import annotations
+
+import pytest
+
+
+def _count_kinds(tree, c=None):
+    c = c if c is not None else {}
+    c[tree[0]] = c.get(tree[0], 0) + 1
+    if tree[0] in ("Union", "Intersection", "Difference"):
+        _count_kinds(tree[1], c)
+        _count_kinds(tree[2], c)
+    return c
+
+
+def _depth(tree):
+    if tree[0] in ("Union", "Intersection", "Difference"):
+        return 1 + max(_depth(tree[1]), _depth(tree[2]))
+    return 0
+
+
+@pytest.mark.parametrize("seed,leaves", [(3, 2), (11, 9), (21, 300), (79, 2048), (191, 2048), (93, 2048),
+                                         (5, 4096), (8, 40)])
+def test_plan_matches_the_rules(csg, seed, leaves):
+    from csgrt import scenes
+    tree = scenes.random_tree(seed, 2, leaves, 12)
+    text = scenes.write_text(tree)
+    plan = csg.plan_tree(text)
+    kinds = _count_kinds(tree)
+    n = sum(kinds.get(k, 0) for k in ("Sphere", "Cylinder", "Cube"))
+    assert plan["n_prims"] == n and plan["n_nodes"] == 2 * n - 1
+    assert plan["op_depth"] == _depth(tree)
+    d = plan["op_depth"]
+    assert plan["stack_class"] == (4 if d <= 4 else 8 if d <= 8 else 12 if d <= 12 else 16 if d <= 15 else 32)
+    assert plan["rolled"] == int(kinds.get("Cylinder", 0) > 0 and n > 8)
+    shift = 0
+    while (n + (1 << shift) - 1) >> shift > 32 * 32:
+        shift += 1
+    assert plan["live_shift"] == shift
+    assert plan["live_words"] == (((n + (1 << shift) - 1) >> shift) + 31) // 32 <= 32
+    fine = plan["rolled"] and shift > 0 and n <= 2048 and (n + 31) // 32 <= 57
+    assert plan["fine_words"] == ((n + 31) // 32 if fine else 0)
+    assert plan["device_bytes"] > 16 * plan["n_nodes"]
+
+
+def test_plan_of_the_reference_files(csg):
+    from conftest import GOLDEN
+    for f in sorted((GOLDEN / "scenes").glob("*.txt")):
+        plan = csg.plan_tree(f.read_text())
+        assert plan["n_nodes"] == 2 * plan["n_prims"] - 1
+        assert plan["fine_words"] == 0  # the reference's own scenes are small
+
+
+def test_plan_errors_are_parse_errors(csg):
+    with pytest.raises(csg.CsgError) as e:
+        csg.plan_tree("Sphere 0 0 0 FF0000")
+    assert e.value.code == csg.CSG_E_PARSE
+    assert csg.lib().csg_tree_plan(b"Sphere 0 0 0 FF0000 1", 21, 0, None, None, 0) == csg.CSG_E_ARG
