@@ -65,7 +65,7 @@ class csg_camera(ctypes.Structure):
 class csg_scene_info(ctypes.Structure):
     _fields_ = [("n_nodes", _i32), ("n_prims", _i32), ("op_depth", _i32), ("stack_class", _i32),
                 ("device_bytes", ctypes.c_uint64), ("rolled", _i32), ("live_words", _i32), ("live_shift", _i32),
-                ("fine_words", _i32)]
+                ("fine_words", _i32), ("short_circuit", _i32)]
 
 
 class csg_planes(ctypes.Structure):

@@ -182,6 +182,7 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.fine_shift = pk.fine_shift;
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
     s->dev.rolled = csgrt::use_rolled(s->tree) ? 1 : 0;
+    s->dev.short_circuit = csgrt::use_short_circuit(s->tree) ? 1 : 0;
     s->status = reinterpret_cast<unsigned long long*>(base + off_status);
     *out = s;
     return CSG_OK;
@@ -212,6 +213,7 @@ int csg_tree_plan(const char* text, size_t len, int32_t flags, csg_scene_info* i
     info->live_words = pk.live_words;
     info->live_shift = pk.live_shift;
     info->fine_words = pk.fine ? pk.fine_words : 0;
+    info->short_circuit = csgrt::use_short_circuit(tree) ? 1 : 0;
     return CSG_OK;
 }
 
@@ -280,6 +282,7 @@ int csg_scene_get_info(const csg_scene* s, csg_scene_info* info)
     info->live_words = s->dev.live_words;
     info->live_shift = s->dev.live_shift;
     info->fine_words = s->dev.fine ? s->dev.fine_words : 0;
+    info->short_circuit = s->dev.short_circuit;
     return CSG_OK;
 }
 

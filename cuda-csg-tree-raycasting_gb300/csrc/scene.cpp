@@ -339,6 +339,18 @@ bool use_rolled(const HostTree& tree)
     return false;
 }
 
+bool use_short_circuit(const HostTree& tree)
+{
+    if (!use_rolled(tree)) return false;
+    size_t ops = 0, decisive = 0;
+    for (const RefNode& n : tree.nodes) {
+        if (n.prim != -1) continue;
+        ++ops;
+        if (n.type == kDifference || n.type == kIntersection) ++decisive;
+    }
+    return 8 * decisive >= ops;
+}
+
 int32_t stack_class_for_depth(int32_t op_depth)
 {
     if (op_depth <= 4) return 4;

@@ -807,6 +807,23 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
     }
 }
 
+// Operator short-circuit (a tuning knob; 1 on).  Kensler's tables give Miss for a
+// Difference whose left child is a Miss and for an Intersection with a Miss child, whatever
+// the other child holds (the Miss rows and columns of those tables are all hMiss), and hMiss
+// resets both records to the default Miss.  The reference still traverses the other child;
+// skipping it changes no output: the node returns the same default Miss, tmin is restored by
+// SaveLft or set by a loop before any later GoTo reads it, and the stacks are left as the
+// skipped traversal would leave them (it pushes and pops in pairs when no stack can
+// overflow, SD < 32; the 32-entry class reproduces the reference's overflow behaviour, so it
+// always traverses).  Skipped subtrees keep their live bits, which only prunes less.
+// Rolled scenes opt in (DeviceScene::short_circuit, chosen by the scene compiler); the
+// unrolled variant, which serves small trees and sphere/cube scenes such as the cheese
+// frame, has no short-circuit code (with it, 3-5% slower there); 0 here removes it.
+#ifndef CSG_SHORT_CIRCUIT
+#define CSG_SHORT_CIRCUIT 1
+#endif
+constexpr bool kShortCircuit = CSG_SHORT_CIRCUIT != 0;
+
 // One iteration of the CSGRayCast loop: SaveLft, GoTo (:514-595), Compute (:597-661) with
 // LookUpActions (:664-706).  `tab` is the 27-entry table in shared memory.
 // ROLLED evaluates GoTo's tests (both children of an operator, or the leaf GoTo landed on)
@@ -825,8 +842,17 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
     st.ntm = T.ntm;
     if (T.action & kSaveL) {
         T.tmin = st.tpop();
-        st.ppush(T.L);
-        T.action = kGotoR;
+        if (kShortCircuit && ROLLED && SD < 32 && sc.short_circuit && (T.L.hit & kMiss) &&
+            (T.ct.w == kDifference || T.ct.w == kIntersection)) {
+            // The left subtree returned a Miss: the node's Compute gives Miss whatever the
+            // right subtree returns, so it is not traversed (the pending LoadL is dropped;
+            // it would reload this same record).
+            T.as.pop();
+            T.action = kCompute;
+        } else {
+            st.ppush(T.L);
+            T.action = kGotoR;
+        }
     }
     if (T.action & (kGotoL | kGotoR)) {
         T.cur = (T.action & kGotoL) ? T.ct.x : T.ct.y;
@@ -886,7 +912,16 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             if (H.hit == kMiss) lm.clear_leaf(T.ct.x);
         }
         if (op) {
-            if (gl || gr) {
+            // A child that is not descended into and holds a Miss is a Miss at this tmin
+            // (a leaf's own test, a culled box or no live leaf).  A Difference whose left
+            // child is such a Miss, or an Intersection with one, computes Miss whatever
+            // the other child returns: go straight to Compute.
+            const bool lmiss = !gl && (T.L.hit & kMiss), rmiss = !gr && (T.R.hit & kMiss);
+            const bool decided = kShortCircuit && ROLLED && SD < 32 && sc.short_circuit &&
+                                 ((T.ct.w == kDifference && lmiss) || (T.ct.w == kIntersection && (lmiss || rmiss)));
+            if (decided) {
+                T.action = kCompute;
+            } else if (gl || gr) {
                 if (!gl) {
                     st.ppush(T.L);
                     T.as.push(kLoadL);

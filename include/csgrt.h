@@ -64,6 +64,8 @@ typedef struct csg_scene_info {
     int32_t live_words;   /* words of the per-ray live-leaf mask (batched renders) */
     int32_t live_shift;   /* log2 of the leaves per mask bit */
     int32_t fine_words;   /* words of the one-bit-per-leaf mask of single-view renders, 0 if unused */
+    int32_t short_circuit;/* the traversal skips the other child of a Difference / Intersection
+                             that a Miss child decides */
 } csg_scene_info;
 
 /* Optional per-pixel planes.  Any pointer may be NULL.  Row-major, w*h entries, row 0 is

@@ -52,7 +52,7 @@ def test_camera_matches_reference_bytes(csg):
 
 def test_camera_struct_layout(csg):
     assert ctypes.sizeof(csg.csg_camera) == 60
-    assert ctypes.sizeof(csg.csg_scene_info) == 40
+    assert ctypes.sizeof(csg.csg_scene_info) == 48
     assert ctypes.sizeof(csg.csg_server_stats) == 88
     c = csg.Camera.from_floats(np.arange(15, dtype=np.float32))
     assert (c.floats() == np.arange(15, dtype=np.float32)).all()

@@ -1,7 +1,8 @@
 """The scene compiler's host-side decisions (csg_tree_plan, no device work): stack class
 from the operator depth, rolled GoTo for trees with cylinders and more than 8 primitives,
 live-mask words and granularity, the fine mask of single-view renders for rolled trees of
-1,025-1,824 leaves, and the device layout size."""
+1,025-1,824 leaves, the operator short-circuit for trees where Differences and
+Intersections are common, and the device layout size."""
 from __future__ import annotations
 
 import pytest
@@ -44,6 +45,9 @@ def test_plan_matches_the_rules(csg, seed, leaves):
     fine = plan["rolled"] and shift > 0 and n <= 2048 and (n + 31) // 32 <= 57
     assert plan["fine_words"] == ((n + 31) // 32 if fine else 0)
     assert plan["device_bytes"] > 16 * plan["n_nodes"]
+    ops = sum(kinds.get(k, 0) for k in ("Union", "Intersection", "Difference"))
+    decisive = kinds.get("Intersection", 0) + kinds.get("Difference", 0)
+    assert plan["short_circuit"] == int(bool(plan["rolled"]) and 8 * decisive >= ops)
 
 
 def test_plan_of_the_reference_files(csg):
@@ -59,3 +63,11 @@ def test_plan_errors_are_parse_errors(csg):
         csg.plan_tree("Sphere 0 0 0 FF0000")
     assert e.value.code == csg.CSG_E_PARSE
     assert csg.lib().csg_tree_plan(b"Sphere 0 0 0 FF0000 1", 21, 0, None, None, 0) == csg.CSG_E_ARG
+
+
+def test_plan_of_the_benchmark_scenes(csg):
+    from csgrt import scenes
+    cheese = csg.plan_tree(scenes.config_scene_text(2, 0))
+    assert cheese["short_circuit"] == 0 and cheese["rolled"] == 0  # one Difference over a Union of spheres
+    assert csg.plan_tree(scenes.config_scene_text(1, 0))["short_circuit"] == 0  # five primitives
+    assert csg.plan_tree(scenes.config_scene_text(3, 0))["short_circuit"] == 1
