@@ -228,6 +228,7 @@ def check(code: int, msg: str = ""):
 
 
 CSG_SCENE_EXACT_BOXES = 1
+CSG_SCENE_FINE_MASK = 2
 
 
 def parse_tree(text: str | bytes, exact_boxes: bool = False):
@@ -249,14 +250,14 @@ def parse_tree(text: str | bytes, exact_boxes: bool = False):
     return nodes, prims, dep.value
 
 
-def plan_tree(text: str | bytes, exact_boxes: bool = False) -> dict:
+def plan_tree(text: str | bytes, exact_boxes: bool = False, fine_mask: bool = False) -> dict:
     """csg_tree_plan: what a Scene built from `text` would hold (sizes, kernel variant, live
     masks), computed on the host alone."""
     data = text.encode() if isinstance(text, str) else bytes(text)
     inf = csg_scene_info()
     err = ctypes.create_string_buffer(512)
-    rc = lib().csg_tree_plan(data, len(data), CSG_SCENE_EXACT_BOXES if exact_boxes else 0, ctypes.byref(inf), err,
-                             512)
+    flags = (CSG_SCENE_EXACT_BOXES if exact_boxes else 0) | (CSG_SCENE_FINE_MASK if fine_mask else 0)
+    rc = lib().csg_tree_plan(data, len(data), flags, ctypes.byref(inf), err, 512)
     if rc != CSG_OK:
         raise CsgError(rc, err.value.decode(errors="replace"))
     return {k: getattr(inf, k) for k, _ in csg_scene_info._fields_}
@@ -327,12 +328,12 @@ def light_dir(polar=None, azimuth=None) -> np.ndarray:
 class Scene:
     """A parsed, device-resident CSG scene (opaque handle)."""
 
-    def __init__(self, text: str | bytes, exact_boxes: bool = False):
+    def __init__(self, text: str | bytes, exact_boxes: bool = False, fine_mask: bool = False):
         data = text.encode() if isinstance(text, str) else bytes(text)
         h = _vp()
         err = ctypes.create_string_buffer(512)
-        rc = lib().csg_scene_create_ex(data, len(data), CSG_SCENE_EXACT_BOXES if exact_boxes else 0, ctypes.byref(h),
-                                       err, 512)
+        flags = (CSG_SCENE_EXACT_BOXES if exact_boxes else 0) | (CSG_SCENE_FINE_MASK if fine_mask else 0)
+        rc = lib().csg_scene_create_ex(data, len(data), flags, ctypes.byref(h), err, 512)
         if rc != CSG_OK:
             raise CsgError(rc, err.value.decode(errors="replace"))
         self.h = h

@@ -121,7 +121,7 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
 int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene** out, char* err, size_t errlen)
 {
     if (!out) return CSG_E_ARG;
-    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
+    if (flags & ~(CSG_SCENE_EXACT_BOXES | CSG_SCENE_FINE_MASK)) return CSG_E_ARG;
     *out = nullptr;
     if (!text && len) return CSG_E_ARG;
     csg_scene* s = new (std::nothrow) csg_scene();
@@ -177,7 +177,7 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.n_bvh = static_cast<int32_t>(pk.bvh.size() / 4);
     s->dev.live_words = pk.live_words;
     s->dev.live_shift = pk.live_shift;
-    s->dev.fine = pk.fine;
+    s->dev.fine = (pk.fine || ((flags & CSG_SCENE_FINE_MASK) && csgrt::fine_mask_possible(s->tree, pk))) ? 1 : 0;
     s->dev.fine_words = pk.fine_words;
     s->dev.fine_shift = pk.fine_shift;
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
@@ -191,7 +191,7 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
 int csg_tree_plan(const char* text, size_t len, int32_t flags, csg_scene_info* info, char* err, size_t errlen)
 {
     if (!info || (!text && len)) return CSG_E_ARG;
-    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
+    if (flags & ~(CSG_SCENE_EXACT_BOXES | CSG_SCENE_FINE_MASK)) return CSG_E_ARG;
     csgrt::HostTree tree;
     std::string msg;
     const int rc = csgrt::parse_tree(std::string_view(text ? text : "", len), tree, msg);
@@ -212,7 +212,8 @@ int csg_tree_plan(const char* text, size_t len, int32_t flags, csg_scene_info* i
     info->rolled = csgrt::use_rolled(tree) ? 1 : 0;
     info->live_words = pk.live_words;
     info->live_shift = pk.live_shift;
-    info->fine_words = pk.fine ? pk.fine_words : 0;
+    const bool fine = pk.fine || ((flags & CSG_SCENE_FINE_MASK) && csgrt::fine_mask_possible(tree, pk));
+    info->fine_words = fine ? pk.fine_words : 0;
     info->short_circuit = csgrt::use_short_circuit(tree) ? 1 : 0;
     return CSG_OK;
 }
@@ -230,7 +231,7 @@ int csg_tree_parse_ex(const char* text, size_t len, int32_t flags, void* nodes44
                       char* err, size_t errlen)
 {
     if (!text && len) return CSG_E_ARG;
-    if (flags & ~CSG_SCENE_EXACT_BOXES) return CSG_E_ARG;
+    if (flags & ~(CSG_SCENE_EXACT_BOXES | CSG_SCENE_FINE_MASK)) return CSG_E_ARG;
     csgrt::HostTree tree;
     std::string msg;
     const int rc = csgrt::parse_tree(std::string_view(text ? text : "", len), tree, msg);

@@ -48,11 +48,11 @@ struct RenderParams {
 constexpr bool kLocalStacks = CSG_TILED_LOCAL_STACKS != 0;
 // Preferred shared-memory carveout in percent of the maximum (a tuning knob; -1 leaves
 // the choice to the driver, which sizes shared memory for the most resident blocks).
-// 80% keeps six blocks per SM for live masks up to ~30 KB per block and gives the largest
-// masks five blocks and a larger L1: 5% faster on the heaviest batch view (1,694 leaves,
-// whose 0.5 MB scene misses L1), within 1% elsewhere; 66% and 50% cost up to 11% and 35%.
+// Before the operator short-circuit, 80% (five blocks and a larger L1 for the largest live
+// masks) was 5% faster on the heaviest batch view; with it, the driver's choice is 3% faster
+// over the batch's 35 largest trees and 5% over its 1,024 views rendered one by one.
 #ifndef CSG_TILED_CARVEOUT
-#define CSG_TILED_CARVEOUT 80
+#define CSG_TILED_CARVEOUT -1
 #endif
 
 // FINE: the scene's fine live mask (scenes with scene.fine set; rolled variants only).

@@ -351,6 +351,11 @@ bool use_short_circuit(const HostTree& tree)
     return 8 * decisive >= ops;
 }
 
+bool fine_mask_possible(const HostTree& tree, const PackedScene& pk)
+{
+    return use_rolled(tree) && pk.live_shift > 0 && pk.fine_shift == 0;
+}
+
 int32_t stack_class_for_depth(int32_t op_depth)
 {
     if (op_depth <= 4) return 4;

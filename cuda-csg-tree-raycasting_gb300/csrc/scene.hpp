@@ -84,16 +84,17 @@ constexpr int kKidsPerNode = 5;
 constexpr int kLiveWordsMax = CSG_LIVE_WORDS_MAX;
 static_assert(kLiveWordsMax >= 1 && kLiveWordsMax <= 64, "live-mask words");
 // Fine live mask of single-view renders (the render_tiled variants for rolled scenes):
-// one bit per leaf, up to kFineWordsMax words, used for a scene whose own mask groups
-// leaves (more than 32 * kLiveWordsMax of them) when the fine mask needs at most
-// CSG_FINE_WORDS_USE words.  Measured on the batched workload's 35 trees of 1,025-2,015
-// leaves, as single views: one bit per leaf up to 1,824 leaves (57 words) is faster for
-// most (up to 20%), the larger ones run up to 13% slower (fewer resident blocks), and a
-// tree of ~3,600 leaves with two leaves per bit instead of four ran 8% slower, so only
-// one bit per leaf is used.  0 disables it.
+// one bit per leaf, up to kFineWordsMax words, for a scene whose own mask groups leaves
+// (more than 32 * kLiveWordsMax of them).  Used by default when the fine mask needs at
+// most CSG_FINE_WORDS_USE words (0: never), and on request (CSG_SCENE_FINE_MASK) up to
+// kFineWordsMax.  Measured on the batched workload's 35 trees of 1,025-2,015 leaves, as
+// single views: before the operator short-circuit, one bit per leaf up to 1,824 leaves
+// took their time down 4.7%; with it, the fine mask made 33 of the 35 slower and their
+// total 9% longer (fewer resident blocks now cost more than the finer pruning saves), so
+// it is off by default.
 constexpr int kFineWordsMax = 64;
 #ifndef CSG_FINE_WORDS_USE
-#define CSG_FINE_WORDS_USE 57
+#define CSG_FINE_WORDS_USE 0
 #endif
 
 struct DeviceScene {
@@ -155,5 +156,9 @@ bool use_rolled(const HostTree& tree);
 // cheese scene (one Difference over a 511-node Union, unrolled variant) the extra tests in
 // every GoTo cost 3-5% and saved nothing, so such trees keep the plain traversal.
 bool use_short_circuit(const HostTree& tree);
+
+// Whether a packed tree can use the fine live mask (rolled variant, grouped own mask, one
+// bit per leaf within kFineWordsMax words).
+bool fine_mask_possible(const HostTree& tree, const PackedScene& pk);
 
 }  // namespace csgrt

@@ -90,6 +90,11 @@ int csg_scene_create(const char* text, size_t len, csg_scene** out, char* err, s
  * the cylinder (the reference's, BVHNode.cuh:34-49, cut hits), each widened by 2^-12 of
  * its size plus 1e-5.  Cube and operator boxes as the reference builds them. */
 #define CSG_SCENE_EXACT_BOXES 1
+/* Fine live mask (same output): single-view renders of a rolled tree of 1,025-2,048 leaves
+ * keep one live bit per leaf instead of one per two leaves.  Off by default: since the
+ * operator short-circuit it is faster for a few trees and slower for most (fewer resident
+ * blocks); a caller rendering one large tree many times can time both. */
+#define CSG_SCENE_FINE_MASK 2
 int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene** out, char* err, size_t errlen);
 /* Frees the scene's device memory (Raycaster::CleanUp, Raycaster.cu:36-44). */
 int csg_scene_destroy(csg_scene* scene);

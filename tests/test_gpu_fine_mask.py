@@ -1,6 +1,7 @@
-"""Single-view renders of large rolled trees run with a one-bit-per-leaf live mask (the
-scene's fine mask); every plane still equals the reference kernel's, bit for bit.  Trees of
-1,173 and 1,694 leaves use it; one of 1,852 leaves keeps its grouped mask."""
+"""Single-view renders of large rolled trees with the one-bit-per-leaf live mask (the
+scene's fine mask, CSG_SCENE_FINE_MASK): every plane still equals the reference kernel's,
+bit for bit, for trees of 1,173, 1,694 and 1,852 leaves; the scene holds what the host-side
+plan says."""
 from __future__ import annotations
 
 import numpy as np
@@ -10,7 +11,7 @@ from test_gpu_parity import assert_bit_exact, engine_render
 
 pytestmark = pytest.mark.gpu
 
-CASES = [(79, True), (191, True), (93, False)]  # (tree seed of the batched workload, fine mask used)
+CASES = [79, 191, 93]  # tree seeds of the batched workload (1,173, 1,694 and 1,852 leaves)
 
 
 def test_fine_mask_trees_vs_reference_kernel(csg):
@@ -22,20 +23,18 @@ def test_fine_mask_trees_vs_reference_kernel(csg):
     G = RefCuda()
     rng = np.random.default_rng(11)
     hits = 0
-    for seed, fine in CASES:
+    for seed in CASES:
         text = scenes.write_text(scenes.random_tree(seed, 2, 2048, 12))
-        with csg.Scene(text) as sc:
+        with csg.Scene(text, fine_mask=True) as sc:
             info = sc.info()
-        assert info == csg.plan_tree(text)  # the host-side plan is what the scene holds
+        assert info == csg.plan_tree(text, fine_mask=True)  # the host-side plan is what the scene holds
         assert info["n_prims"] > 1024 and info["rolled"] == 1 and info["live_shift"] == 1, (seed, info)
-        assert (info["fine_words"] > 0) == fine, (seed, info)
-        if fine:
-            assert info["fine_words"] == (info["n_prims"] + 31) // 32
+        assert info["fine_words"] == (info["n_prims"] + 31) // 32, (seed, info)
         for _ in range(2):
             cam = csg.Camera.look_at_origin(scenes.seeded_direction(rng), float(rng.uniform(2.5, 4.0))).floats()
             light = csg.light_dir()
             w, h = 256, 192
-            eng = engine_render(csg, text, cam, light, w, h)
+            eng = engine_render(csg, text, cam, light, w, h, fine_mask=True)
             nodes44, prims48, _ = csg.parse_tree(text)
             ref = G.render(nodes44, prims48, cam, light, w, h)
             ref["rgba8"] = quantize_rgba8(ref["rgba"])

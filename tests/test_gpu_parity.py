@@ -39,10 +39,11 @@ def refcuda():
     return RefCuda()
 
 
-def engine_render(csg, text, cam_floats, light, w, h, planes=("rgba8", "t", "prim", "normal", "rgba32f")):
+def engine_render(csg, text, cam_floats, light, w, h, planes=("rgba8", "t", "prim", "normal", "rgba32f"),
+                  fine_mask=False):
     import torch
     cam = csg.Camera.from_floats(cam_floats)
-    with csg.Scene(text) as sc:
+    with csg.Scene(text, fine_mask=fine_mask) as sc:
         out = sc.render_torch(cam, light, w, h, planes=planes)
         torch.cuda.synchronize()
         assert sc.check() == 0

@@ -1,7 +1,7 @@
 """The scene compiler's host-side decisions (csg_tree_plan, no device work): stack class
 from the operator depth, rolled GoTo for trees with cylinders and more than 8 primitives,
-live-mask words and granularity, the fine mask of single-view renders for rolled trees of
-1,025-1,824 leaves, the operator short-circuit for trees where Differences and
+live-mask words and granularity, the fine mask of single-view renders (on request) for
+rolled trees of 1,025-2,048 leaves, the operator short-circuit for trees where Differences and
 Intersections are common, and the device layout size."""
 from __future__ import annotations
 
@@ -42,8 +42,12 @@ def test_plan_matches_the_rules(csg, seed, leaves):
         shift += 1
     assert plan["live_shift"] == shift
     assert plan["live_words"] == (((n + (1 << shift) - 1) >> shift) + 31) // 32 <= 32
-    fine = plan["rolled"] and shift > 0 and n <= 2048 and (n + 31) // 32 <= 57
-    assert plan["fine_words"] == ((n + 31) // 32 if fine else 0)
+    possible = bool(plan["rolled"]) and shift > 0 and n <= 2048
+    if plan["fine_words"]:  # by default only where the build's threshold allows
+        assert possible and plan["fine_words"] == (n + 31) // 32
+    asked = csg.plan_tree(text, fine_mask=True)  # CSG_SCENE_FINE_MASK
+    assert asked["fine_words"] == ((n + 31) // 32 if possible else 0)
+    assert {k: v for k, v in asked.items() if k != "fine_words"} == {k: v for k, v in plan.items() if k != "fine_words"}
     assert plan["device_bytes"] > 16 * plan["n_nodes"]
     ops = sum(kinds.get(k, 0) for k in ("Union", "Intersection", "Difference"))
     decisive = kinds.get("Intersection", 0) + kinds.get("Difference", 0)
