@@ -67,6 +67,8 @@ class Oracle:
                            _vp, _vp, _vp, _vp, _vp, _vp]
             fn.restype = _i
         L.orc_tan_half_fov.argtypes = [_f]
+        L.orc_set_short_circuit.argtypes = [_i]
+        L.orc_set_short_circuit.restype = None
         L.orc_boxes_exact.argtypes = [_vp, _i, _vp]
         L.orc_boxes_exact.restype = None
         L.orc_tan_half_fov.restype = _f
@@ -128,6 +130,10 @@ class Oracle:
         else:
             self.lib.orc_light_dir(polar, azimuth, _ptr(out))
         return out
+
+    def set_short_circuit(self, on: bool):
+        """The engine's operator short-circuit in the traversal (off: the reference's own)."""
+        self.lib.orc_set_short_circuit(1 if on else 0)
 
     def tan_half_fov(self, fov: float) -> float:
         return float(np.float32(self.lib.orc_tan_half_fov(fov)))

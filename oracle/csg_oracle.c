@@ -476,6 +476,15 @@ float orc_tan_half_fov(float fov)
 static __thread uint64_t orc_flop_counter;
 #define ORC_FL(n) (orc_flop_counter += (uint64_t)(n))
 
+/* Optional operator short-circuit (not the reference's algorithm; off by default): a
+ * Difference whose left child, or an Intersection with a child, is a Miss already known at
+ * GoTo, and a Difference / Intersection whose left subtree returned a Miss, go straight to
+ * Compute without traversing the other child -- the engine's rule for trees whose stacks
+ * cannot overflow.  The tests render with and without it and compare every plane, a check
+ * of that rule independent of the GPU. */
+static int orc_short_circuit;
+void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
+
 #define ORC_FMA 0
 #define ORC_SUFFIX(name) name##_ieee
 #include "csg_oracle_render.inc"

@@ -119,6 +119,10 @@ int orc_render_list_fma(const orc_node* nodes, int n_nodes, const orc_prim* prim
                         uint8_t* hit, float* t, int32_t* prim, float* normal3,
                         uint32_t* rgba8, orc_counts* counts);
 
+/* Optional operator short-circuit of the traversal (off by default; not the reference's
+ * algorithm): see csg_oracle.c.  Process-wide. */
+void orc_set_short_circuit(int on);
+
 #ifdef __cplusplus
 }
 #endif
