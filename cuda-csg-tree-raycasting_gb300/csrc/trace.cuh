@@ -526,18 +526,24 @@ struct LocalStacks {
 };
 
 // Per-ray live-leaf mask.  Bit g stands for leaves [g << shift, (g + 1) << shift); a
-// clear bit means every leaf of the group is known to return Miss for every tmin the
-// traversal can still use.  That is sound because a leaf's result is monotone in tmin
-// (a Miss stays a Miss when tmin grows: a sphere needs a root beyond tmin, a cylinder a
-// valid branch beyond tmin, a box tmx beyond tmin), and the tmin with which the traversal
-// reaches any node never decreases (loops only move tmin forward, SaveLft restores the
-// tmin the parent was entered with).  A subtree whose leaves are all Miss evaluates to a
-// Miss whether or not it is traversed, and a Miss's t and index reach no decision and no
-// output, so skipping such a subtree changes nothing.  Bits are cleared when a leaf test
-// returns Miss and when an operator child's box culls (its leaves' boxes are nested in
-// it, so they cull too).  The mask lives in shared memory, word k of a lane at
-// w[k * nt]; `sum` has bit k set while word k is non-zero (SumT: 32 bits for masks of up
-// to 32 words, 64 bits for up to 64).
+// clear bit means every leaf of the group is known to return Miss at the tmin of any
+// later visit.  A leaf's result is monotone in tmin (a Miss stays a Miss when tmin grows:
+// a sphere needs a root beyond tmin, a cylinder a valid branch beyond tmin, a box tmx
+// beyond tmin), so a bit cleared at tmin t stays valid while visits come with tmin >= t.
+// The pre-pass clears at tmin = 0, below every tmin.  Bits are also cleared during the
+// traversal, when a leaf test returns Miss and when an operator child's box culls (its
+// leaves' boxes are nested in it, so they cull too), and those hold only as long as tmin
+// does not fall below the tmin of the clear.  It can fall: a node returns its closer
+// child's t, which can lie below a tmin its other child's subtree has already looped to,
+// and a loop of an ancestor then re-enters that subtree with the lower tmin (the
+// reference does this on about one ray in several hundred of random trees).  Subtrees
+// are re-entered only through loops, so `tclr` keeps the largest tmin of any traversal
+// clear, and a loop whose new tmin is below it marks the looped child's leaves live again
+// (restore_range), which only prunes less.  A subtree whose leaves are all Miss
+// evaluates to a Miss whether or not it is traversed, and a Miss's t and index reach no
+// decision and no output, so skipping such a subtree changes nothing.  The mask lives in
+// shared memory, word k of a lane at w[k * nt]; `sum` has bit k set while word k is
+// non-zero (SumT: 32 bits for masks of up to 32 words, 64 bits for up to 64).
 using live_sum_t = std::conditional<(kLiveWordsMax > 32), unsigned long long, uint32_t>::type;
 
 template <typename SumT>
@@ -548,6 +554,7 @@ struct LiveMaskT {
     int shift;
     int words;
     live_sum_t sum;
+    float tclr;  // largest tmin of a clear made during the traversal (-inf: none)
 
     __device__ __forceinline__ uint32_t& word(int k) { return w[k * nt]; }
     __device__ __forceinline__ void fill(int n_groups)
@@ -589,21 +596,38 @@ struct LiveMaskT {
         word(k) = v;
         if (!v) sum &= ~((live_sum_t)1 << k);
     }
-    __device__ __forceinline__ void clear_leaf(int leaf)
+    __device__ __forceinline__ void clear_leaf(int leaf, float tmin)
     {
-        if (shift == 0) clear_word(leaf >> 5, 1u << (leaf & 31));
+        if (shift == 0) {
+            clear_word(leaf >> 5, 1u << (leaf & 31));
+            tclr = fmaxf(tclr, tmin == tmin ? tmin : INFINITY);
+        }
     }
     // Clears the groups lying entirely inside [lo, hi].
-    __device__ __forceinline__ void clear_range(int lo, int hi)
+    __device__ __forceinline__ void clear_range(int lo, int hi, float tmin)
     {
         const int ga = (lo + (1 << shift) - 1) >> shift, gb = ((hi + 1) >> shift) - 1;
         if (ga > gb) return;
+        tclr = fmaxf(tclr, tmin == tmin ? tmin : INFINITY);  // a NaN tmin: restore at every loop
         const int wa = ga >> 5, wb = gb >> 5;
         for (int k = wa; k <= wb; ++k) {
             if (!((sum >> k) & 1u)) continue;
             const uint32_t lo_m = (k == wa) ? (0xffffffffu << (ga & 31)) : 0xffffffffu;
             const uint32_t hi_m = (k == wb) ? (0xffffffffu >> (31 - (gb & 31))) : 0xffffffffu;
             clear_word(k, lo_m & hi_m);
+        }
+    }
+    // Sets every group that holds a leaf of [lo, hi] (groups reaching outside the range
+    // too: more live bits only prune less).
+    __device__ __forceinline__ void restore_range(int lo, int hi)
+    {
+        const int ga = lo >> shift, gb = hi >> shift;
+        const int wa = ga >> 5, wb = gb >> 5;
+        for (int k = wa; k <= wb; ++k) {
+            const uint32_t lo_m = (k == wa) ? (0xffffffffu << (ga & 31)) : 0xffffffffu;
+            const uint32_t hi_m = (k == wb) ? (0xffffffffu >> (31 - (gb & 31))) : 0xffffffffu;
+            word(k) |= lo_m & hi_m;
+            sum |= (live_sum_t)1 << k;
         }
     }
 };
@@ -647,6 +671,7 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
                                              int* wstack)
 {
     const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
+    lm.tclr = -INFINITY;
     if (!sc.prepass || sc.n_bvh == 0) {
         lm.fill(n_groups);
         return;
@@ -734,7 +759,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
         const bool go = box_hit(ray, lo, hi, tmin);
         if (!go) {
             H.hit = kMiss;
-            lm.clear_range(leaf_lo, leaf_hi);
+            lm.clear_range(leaf_lo, leaf_hi, tmin);
         }
         return go;
     }
@@ -755,7 +780,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
     } else {
         H = hit_default();
     }
-    if (H.hit == kMiss) lm.clear_leaf(prim);
+    if (H.hit == kMiss) lm.clear_leaf(prim, tmin);
     return false;
 }
 
@@ -805,6 +830,16 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
         T.cur = -1;
         T.ct = make_int4(0, 0, 0, kUnion);
     }
+}
+
+// A loop re-enters one child of operator `node` with a tmin below that of a traversal
+// clear: its leaves become live again (the leaf ranges are the node's kids record).
+template <class LM>
+__device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restrict__ kids, int node, bool right)
+{
+    const int4 rg = __ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * node + 4]));
+    if (right) lm.restore_range(rg.z, rg.w);
+    else lm.restore_range(rg.x & 0x3fffffff, rg.y);
 }
 
 // Operator short-circuit (a tuning knob; 1 on).  Kensler's tables give Miss for a
@@ -909,7 +944,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
         } else {
             Hit& H = (T.action & kGotoL) ? T.L : T.R;
             hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
-            if (H.hit == kMiss) lm.clear_leaf(T.ct.x);
+            if (H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
         }
         if (op) {
             // A child that is not descended into and holds a Miss is a Miss at this tmin
@@ -969,11 +1004,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             tracer_parent(T, topo);
         } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
             T.tmin = T.L.t;
+            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false);
             st.ppush(T.R);
             T.as.push(kLoadR);
             T.action = kGotoL;
         } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
             T.tmin = T.R.t;
+            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true);
             st.ppush(T.L);
             T.as.push(kLoadL);
             T.action = kGotoR;

@@ -69,6 +69,8 @@ class Oracle:
         L.orc_tan_half_fov.argtypes = [_f]
         L.orc_set_short_circuit.argtypes = [_i]
         L.orc_set_short_circuit.restype = None
+        L.orc_set_live_pruning.argtypes = [_i]
+        L.orc_set_live_pruning.restype = None
         L.orc_boxes_exact.argtypes = [_vp, _i, _vp]
         L.orc_boxes_exact.restype = None
         L.orc_tan_half_fov.restype = _f
@@ -134,6 +136,11 @@ class Oracle:
     def set_short_circuit(self, on: bool):
         """The engine's operator short-circuit in the traversal (off: the reference's own)."""
         self.lib.orc_set_short_circuit(1 if on else 0)
+
+    def set_live_pruning(self, mode: int):
+        """The engine's live-leaf pruning in the traversal: 0 off (the reference's own),
+        1 the engine's rule, 2 the rule without its loop restore (unsound)."""
+        self.lib.orc_set_live_pruning(int(mode))
 
     def tan_half_fov(self, fov: float) -> float:
         return float(np.float32(self.lib.orc_tan_half_fov(fov)))

@@ -485,6 +485,74 @@ static __thread uint64_t orc_flop_counter;
 static int orc_short_circuit;
 void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
 
+/* Optional live-leaf pruning (not the reference's algorithm; off by default): the
+ * engine's rule, restated so that the tests can check it against the reference's
+ * traversal on the CPU.  Each ray starts with a mask over leaf groups (one bit per
+ * 2^shift leaves in preorder, at most ORC_LIVE_GROUPS groups) holding the leaves whose
+ * own box passes at tmin = 0 and whose primitive test at tmin = 0 is not a Miss (a cube:
+ * its box alone).  GoTo treats a child without a live leaf as a Miss without testing it;
+ * a culled operator child clears the groups inside its leaf range and a leaf that returns
+ * Miss its own bit (single-leaf groups only), recording the largest tmin of such a clear;
+ * a loop whose new tmin is below that tmin marks the looped child's groups live again.
+ * Mode 1 is that rule; mode 2 leaves out the loop restore (an unsound rule, kept so that
+ * a test can show what the restore prevents).  Process-wide. */
+#define ORC_LIVE_GROUPS 1024
+static int orc_live_mode;
+static int* orc_live_lo;
+static int* orc_live_hi;
+static int orc_live_cap, orc_live_shift, orc_live_nodes;
+void orc_set_live_pruning(int mode) { orc_live_mode = (mode == 1 || mode == 2) ? mode : 0; }
+
+/* Leaf ranges (first and last primitive in preorder) of every node, and the group
+ * shift, for the tree about to be rendered. */
+static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
+{
+    if (!orc_live_mode) return 0;
+    if (n_nodes > orc_live_cap) {
+        int* lo = (int*)realloc(orc_live_lo, sizeof(int) * (size_t)n_nodes);
+        if (!lo) return -1;
+        orc_live_lo = lo;
+        int* hi = (int*)realloc(orc_live_hi, sizeof(int) * (size_t)n_nodes);
+        if (!hi) return -1;
+        orc_live_hi = hi;
+        orc_live_cap = n_nodes;
+    }
+    for (int i = n_nodes - 1; i >= 0; --i) {
+        if (nodes[i].prim != -1) {
+            orc_live_lo[i] = orc_live_hi[i] = nodes[i].prim;
+        } else {
+            orc_live_lo[i] = orc_live_lo[nodes[i].left];
+            orc_live_hi[i] = orc_live_hi[nodes[i].right];
+        }
+    }
+    int sh = 0;
+    while (((n_prims + (1 << sh) - 1) >> sh) > ORC_LIVE_GROUPS) ++sh;
+    orc_live_shift = sh;
+    orc_live_nodes = n_nodes;
+    return 0;
+}
+
+typedef struct { uint64_t w[ORC_LIVE_GROUPS / 64]; double tclr; } orc_live;
+static int orc_live_any(const orc_live* m, int lo, int hi)
+{
+    for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g)
+        if ((m->w[g >> 6] >> (g & 63)) & 1u) return 1;
+    return 0;
+}
+static void orc_live_clear(orc_live* m, int lo, int hi, double tmin)
+{
+    const int sh = orc_live_shift;
+    const int ga = (lo + (1 << sh) - 1) >> sh, gb = ((hi + 1) >> sh) - 1;
+    if (ga > gb) return;
+    for (int g = ga; g <= gb; ++g) m->w[g >> 6] &= ~(1ull << (g & 63));
+    const double tc = (tmin == tmin) ? tmin : INFINITY;
+    if (tc > m->tclr) m->tclr = tc;
+}
+static void orc_live_restore(orc_live* m, int lo, int hi)
+{
+    for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g) m->w[g >> 6] |= 1ull << (g & 63);
+}
+
 #define ORC_FMA 0
 #define ORC_SUFFIX(name) name##_ieee
 #include "csg_oracle_render.inc"

@@ -1,0 +1,50 @@
+"""Rays on which the reference re-enters a subtree with a tmin below one the subtree has
+already looped to (a node returns its closer child's t, below a tmin its other child's
+subtree reached, and an ancestor's loop re-descends with it).  A live-leaf mask that keeps
+bits cleared at the higher tmin changes these rays; the engine marks the looped child's
+leaves live again and must match the oracle and the reference kernel bit for bit.  The
+trees and views are ones where the oracle without that restore differs
+(tests/test_live_pruning.py)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from test_gpu_parity import assert_bit_exact, engine_render
+from test_live_pruning import REENTRY_DIR, REENTRY_DIST, REENTRY_TREE
+
+pytestmark = pytest.mark.gpu
+
+
+def _cases():
+    import csgrt
+    from csgrt import scenes
+    out = [(REENTRY_TREE, csgrt.Camera.look_at_origin(np.array(REENTRY_DIR), REENTRY_DIST).floats())]
+    # two more trees of a seeded sweep (tree seed 20000 + i, the i-th view of that sweep)
+    rng = np.random.default_rng(20000)
+    for i in range(142):
+        d, dist = scenes.seeded_direction(rng), float(rng.uniform(2.5, 4.0))
+        if i in (113, 141):
+            out.append((20000 + i, csgrt.Camera.look_at_origin(d, dist).floats()))
+    return out
+
+
+@pytest.mark.parametrize("size", [(48, 36), (96, 72)])
+def test_reentry_rays_match_oracle_and_reference_kernel(csg, oracle, size):
+    from oracle import RefCuda, quantize_rgba8
+    from csgrt import scenes
+    w, h = size
+    light = np.float32(csg.light_dir())
+    G = RefCuda() if RefCuda.available() else None
+    for seed, cam in _cases():
+        text = scenes.write_text(scenes.random_tree(seed, 2, 2048, 12))
+        eng = engine_render(csg, text, cam, light, w, h)
+        nodes, prims = oracle.parse(text)
+        thf = csg.device_tan_half_fov(float(cam[5]))
+        ref = oracle.render(nodes, prims, cam, light, w, h, mode="fma", tan_half_fov=thf)
+        assert_bit_exact(eng, ref, f"tree {seed} {w}x{h} vs oracle")
+        if G is not None:
+            nodes44, prims48, _ = csg.parse_tree(text)
+            k = G.render(nodes44, prims48, cam, light, w, h)
+            k["rgba8"] = quantize_rgba8(k["rgba"])
+            assert_bit_exact(eng, k, f"tree {seed} {w}x{h} vs reference kernel")
