@@ -104,7 +104,8 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     lm.words = FINE ? p.scene.fine_words : p.scene.live_words;
     lm.sum = 0;
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h, frame);
-    dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);
+    // (the 32-entry class traverses without the mask: dev::kPrune)
+    if constexpr (dev::kPrune<SD>) dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
     bool capped = false;
     const dev::Hit h = dev::csg_traverse<SD, ROLLED>(p.scene, ray, st, tab, lm, iter_cap, &capped);

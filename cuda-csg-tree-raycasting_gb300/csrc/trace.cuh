@@ -745,12 +745,13 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 //
 // With boxed == false the same code serves GoTo landing on a leaf (the root is a leaf, or a
 // loop re-enters a leaf child), where the reference calls hitPrimitive with no box test.
-template <class LM>
+// PRUNE: consult and update the live mask (kPrune<SD>).
+template <bool PRUNE, class LM>
 __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restrict__ geo, float4 lo, float4 hi,
                                            int leaf_lo, int leaf_hi, Hit& H, float tmin, LM& lm,
                                            bool boxed = true)
 {
-    if (!lm.any(leaf_lo, leaf_hi)) {
+    if (PRUNE && !lm.any(leaf_lo, leaf_hi)) {
         H.hit = kMiss;
         return false;
     }
@@ -759,7 +760,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
         const bool go = box_hit(ray, lo, hi, tmin);
         if (!go) {
             H.hit = kMiss;
-            lm.clear_range(leaf_lo, leaf_hi, tmin);
+            if (PRUNE) lm.clear_range(leaf_lo, leaf_hi, tmin);
         }
         return go;
     }
@@ -780,7 +781,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
     } else {
         H = hit_default();
     }
-    if (H.hit == kMiss) lm.clear_leaf(prim, tmin);
+    if (PRUNE && H.hit == kMiss) lm.clear_leaf(prim, tmin);
     return false;
 }
 
@@ -831,6 +832,15 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
         T.ct = make_int4(0, 0, 0, kUnion);
     }
 }
+
+// Live-leaf pruning per stack class.  Skipping a subtree leaves out pushes and pops that
+// come in pairs only while no stack can overflow: the classes below 32 entries are chosen
+// so that none can, and the 32-entry class, which reproduces the reference's drop-on-full
+// stacks for trees deeper than 15 operator levels, traverses every subtree as the
+// reference does (pruned, the oracle's renders of such trees change wherever a stack
+// overflows).
+template <int SD>
+constexpr bool kPrune = SD < 32;
 
 // A loop re-enters one child of operator `node` with a tmin below that of a traversal
 // clear: its leaves become live again (the leaf ranges are the node's kids record).
@@ -923,7 +933,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
                 }
                 const bool right = (j == 1) || leaf_right;
                 Hit H = right ? T.R : T.L;
-                const bool go = child_test(T.ray, geo, lo, hi, rlo, rhi, H, T.tmin, lm, op);
+                const bool go = child_test<kPrune<SD>>(T.ray, geo, lo, hi, rlo, rhi, H, T.tmin, lm, op);
                 if (right) {
                     T.R = H;
                     gr = go;
@@ -939,12 +949,12 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             const float4 k2 = __ldg(&kn[2]);
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
-            gl = child_test(T.ray, geo, k0, k1, rg.x & 0x3fffffff, rg.y, T.L, T.tmin, lm);
-            gr = child_test(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
+            gl = child_test<kPrune<SD>>(T.ray, geo, k0, k1, rg.x & 0x3fffffff, rg.y, T.L, T.tmin, lm);
+            gr = child_test<kPrune<SD>>(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
         } else {
             Hit& H = (T.action & kGotoL) ? T.L : T.R;
             hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
-            if (H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
+            if (kPrune<SD> && H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
         }
         if (op) {
             // A child that is not descended into and holds a Miss is a Miss at this tmin
@@ -1004,13 +1014,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             tracer_parent(T, topo);
         } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
             T.tmin = T.L.t;
-            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false);
+            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false);
             st.ppush(T.R);
             T.as.push(kLoadR);
             T.action = kGotoL;
         } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
             T.tmin = T.R.t;
-            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true);
+            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true);
             st.ppush(T.L);
             T.as.push(kLoadL);
             T.action = kGotoR;

@@ -494,19 +494,23 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * a culled operator child clears the groups inside its leaf range and a leaf that returns
  * Miss its own bit (single-leaf groups only), recording the largest tmin of such a clear;
  * a loop whose new tmin is below that tmin marks the looped child's groups live again.
- * Mode 1 is that rule; mode 2 leaves out the loop restore (an unsound rule, kept so that
- * a test can show what the restore prevents).  Process-wide. */
+ * The engine prunes only trees of at most 15 operator levels, whose stacks cannot
+ * overflow (deeper trees keep the reference's drop-on-full 32-entry stacks, and skipping
+ * a subtree would change which pushes are dropped).  Mode 1 is that rule; two unsound
+ * variants are kept so that tests can show what the rule's parts prevent: mode 2 leaves
+ * out the loop restore, mode 3 prunes trees of any depth.  Process-wide. */
 #define ORC_LIVE_GROUPS 1024
 static int orc_live_mode;
 static int* orc_live_lo;
 static int* orc_live_hi;
-static int orc_live_cap, orc_live_shift, orc_live_nodes;
-void orc_set_live_pruning(int mode) { orc_live_mode = (mode == 1 || mode == 2) ? mode : 0; }
+static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_active;
+void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 3) ? mode : 0; }
 
 /* Leaf ranges (first and last primitive in preorder) of every node, and the group
  * shift, for the tree about to be rendered. */
 static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
 {
+    orc_live_active = 0;
     if (!orc_live_mode) return 0;
     if (n_nodes > orc_live_cap) {
         int* lo = (int*)realloc(orc_live_lo, sizeof(int) * (size_t)n_nodes);
@@ -529,6 +533,17 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
     while (((n_prims + (1 << sh) - 1) >> sh) > ORC_LIVE_GROUPS) ++sh;
     orc_live_shift = sh;
     orc_live_nodes = n_nodes;
+    /* operator depth: operators on the longest root-to-leaf path (parents precede
+     * their children in preorder) */
+    int depth = 0;
+    int* d = (int*)malloc(sizeof(int) * (size_t)n_nodes);
+    if (!d) return -1;
+    for (int i = 0; i < n_nodes; ++i) {
+        d[i] = (nodes[i].parent >= 0 ? d[nodes[i].parent] : 0) + (nodes[i].prim == -1 ? 1 : 0);
+        if (d[i] > depth) depth = d[i];
+    }
+    free(d);
+    orc_live_active = (orc_live_mode == 3) || depth <= 15;
     return 0;
 }
 

@@ -124,8 +124,8 @@ int orc_render_list_fma(const orc_node* nodes, int n_nodes, const orc_prim* prim
 void orc_set_short_circuit(int on);
 
 /* Optional live-leaf pruning of the traversal (0 off, the default; 1 the engine's rule;
- * 2 the same without its loop restore, an unsound rule): see csg_oracle.c.
- * Process-wide. */
+ * 2 the same without its loop restore and 3 the same on trees of any depth, both
+ * unsound): see csg_oracle.c.  Process-wide. */
 void orc_set_live_pruning(int mode);
 
 #ifdef __cplusplus

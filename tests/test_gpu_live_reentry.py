@@ -4,14 +4,15 @@ subtree reached, and an ancestor's loop re-descends with it).  A live-leaf mask 
 bits cleared at the higher tmin changes these rays; the engine marks the looped child's
 leaves live again and must match the oracle and the reference kernel bit for bit.  The
 trees and views are ones where the oracle without that restore differs
-(tests/test_live_pruning.py)."""
+(tests/test_live_pruning.py).  Also: trees deeper than 15 operator levels, whose 32-entry
+stacks overflow, where the engine must traverse every subtree as the reference does."""
 from __future__ import annotations
 
 import numpy as np
 import pytest
 
 from test_gpu_parity import assert_bit_exact, engine_render
-from test_live_pruning import REENTRY_DIR, REENTRY_DIST, REENTRY_TREE
+from test_live_pruning import DEEP_SEEDS, REENTRY_DIR, REENTRY_DIST, REENTRY_TREE, deep_tree
 
 pytestmark = pytest.mark.gpu
 
@@ -48,3 +49,21 @@ def test_reentry_rays_match_oracle_and_reference_kernel(csg, oracle, size):
             k = G.render(nodes44, prims48, cam, light, w, h)
             k["rgba8"] = quantize_rgba8(k["rgba"])
             assert_bit_exact(eng, k, f"tree {seed} {w}x{h} vs reference kernel")
+
+
+def test_deep_trees_with_overflowing_stacks_match_oracle(csg, oracle):
+    """The reference kernel is not run here: its stacks read uninitialised slots when
+    they overflow; the oracle defines those slots as the engine does."""
+    from csgrt import scenes
+    light = np.float32(csg.light_dir())
+    for seed in DEEP_SEEDS:
+        tree, direction = deep_tree(seed)
+        text = scenes.write_text(tree)
+        with csg.Scene(text) as sc:
+            assert sc.info()["stack_class"] == 32
+        cam = csg.Camera.look_at_origin(direction, 3.0).floats()
+        eng = engine_render(csg, text, cam, light, 80, 60)
+        nodes, prims = oracle.parse(text)
+        thf = csg.device_tan_half_fov(float(cam[5]))
+        ref = oracle.render(nodes, prims, cam, light, 80, 60, mode="fma", tan_half_fov=thf)
+        assert_bit_exact(eng, ref, f"deep tree {seed}")

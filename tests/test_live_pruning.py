@@ -7,8 +7,10 @@ while the iteration count falls.
 
 Without the loop restore the rule is unsound: a node can return its closer child's t, below
 a tmin its other child's subtree has already looped to, and an ancestor's loop then re-enters
-that subtree with the lower tmin, where a leaf cleared at the higher tmin can hit.  The
-last test renders a tree and view where that happens and shows the difference."""
+that subtree with the lower tmin, where a leaf cleared at the higher tmin can hit.  On trees
+deeper than 15 operator levels, whose 32-entry stacks can overflow, skipping a subtree
+changes which pushes are dropped, so the engine does not prune those.  Two tests render
+trees and views where each part of the rule matters and show the difference."""
 from __future__ import annotations
 
 import numpy as np
@@ -20,6 +22,22 @@ PLANES = ("hit", "t", "prim", "normal", "rgba8")
 REENTRY_TREE = 5174
 REENTRY_DIR = (0.8142095647293127, -0.17626529223304066, -0.5531666398629836)
 REENTRY_DIST = 2.5151785211371585
+
+
+# Deep trees: a chain of 30 operators whose other children are leaves or small subtrees.
+DEEP_SEEDS = (3, 11)
+
+
+def deep_tree(seed: int, n_ops: int = 30):
+    """(tree, view direction) for a seeded chain of n_ops operators."""
+    from csgrt import scenes
+    r = np.random.default_rng(seed)
+    t = scenes._random_leaf(r)
+    for _ in range(n_ops):
+        op = scenes.OPERATORS[int(r.integers(0, 3))]
+        other = scenes._random_leaf(r) if r.random() < 0.7 else scenes._random_shape(r, int(r.integers(2, 6)), 3)
+        t = (op, t, other) if r.random() < 0.5 else (op, other, t)
+    return t, scenes.seeded_direction(r)
 
 
 def _render(oracle, nodes, prims, cam, light, w, h, live, sc):
@@ -80,3 +98,20 @@ def test_live_pruning_reentry_case(csg, oracle):
         ref = _render(oracle, nodes, prims, cam, light, 48, 36, 0, sc)
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 1, sc)) == 0
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 2, sc)) > 0
+
+
+def test_deep_trees_are_not_pruned(csg, oracle):
+    """The rule leaves trees deeper than 15 operator levels alone; pruning them anyway
+    changes the renders wherever a 32-entry stack overflows."""
+    from csgrt import scenes
+    light = np.float32(csg.light_dir())
+    for seed in DEEP_SEEDS:
+        tree, direction = deep_tree(seed)
+        assert scenes.op_depth(tree) > 15
+        nodes, prims = oracle.parse(scenes.write_text(tree))
+        cam = csg.Camera.look_at_origin(direction, 3.0).floats()
+        ref = _render(oracle, nodes, prims, cam, light, 40, 30, 0, False)
+        assert int(ref["counts"]["max_actions"].max()) >= 32  # the action stack fills
+        assert int(ref["hit"].sum()) > 50
+        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 1, False)) == 0
+        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 3, False)) > 0
