@@ -115,3 +115,36 @@ def test_deep_trees_are_not_pruned(csg, oracle):
         assert int(ref["hit"].sum()) > 50
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 1, False)) == 0
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 3, False)) > 0
+
+
+def test_live_pruning_with_non_finite_parameters(csg, oracle):
+    """Scenes whose text carries nan, inf or huge values (the parser accepts them, as the
+    reference's std::stof does): hits with NaN t and loops to a NaN tmin keep the rule
+    exact (a NaN tmin counts as below every clear, so the looped child is re-enabled).
+    Some such scenes have rays whose traversal never ends (the oracle stops them at its
+    iteration cap, as the engine does; the reference has none): those scenes are left out."""
+    from csgrt import scenes
+    rng = np.random.default_rng(3)
+    light = np.float32(csg.light_dir())
+    specials = ["nan", "inf", "-inf", "1e38", "-1e38", "0"]
+    rendered = nan_hits = 0
+    for s in range(80):
+        toks = scenes.write_text(scenes.random_tree(9000 + s, 2, 200, 10)).split()
+        slots = [i for i, t in enumerate(toks) if t not in scenes.OPERATORS + scenes.PRIMITIVES and len(t) != 6]
+        for _ in range(int(rng.integers(1, 4))):
+            toks[slots[int(rng.integers(len(slots)))]] = specials[int(rng.integers(len(specials)))]
+        cam = csg.Camera.look_at_origin(scenes.seeded_direction(rng), 3.0).floats()
+        try:
+            nodes, prims = oracle.parse(" ".join(toks))
+        except Exception:  # an out-of-range rotation: the reference rejects it too
+            continue
+        sc = bool(s & 1)
+        ref = _render(oracle, nodes, prims, cam, light, 32, 24, 0, sc)
+        if ref["capped"]:
+            continue  # rays that never end: the reference's loop has no iteration cap
+        got = _render(oracle, nodes, prims, cam, light, 32, 24, 1, sc)
+        assert got["capped"] == 0
+        assert _differ(ref, got) == 0, s
+        rendered += 1
+        nan_hits += int(np.isnan(ref["t"][ref["hit"] != 0]).sum())
+    assert rendered >= 40 and nan_hits > 0
