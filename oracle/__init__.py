@@ -140,7 +140,8 @@ class Oracle:
     def set_live_pruning(self, mode: int):
         """The engine's live-leaf pruning in the traversal: 0 off (the reference's own),
         1 the engine's rule, 2 the rule without its loop restore, 3 the rule on trees of
-        any depth (2 and 3 are unsound)."""
+        any depth (2 and 3 are unsound), 4 the rule with one restore record per region of
+        four mask words (not yet in the engine)."""
         self.lib.orc_set_live_pruning(int(mode))
 
     def tan_half_fov(self, fov: float) -> float:

@@ -498,13 +498,16 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * overflow (deeper trees keep the reference's drop-on-full 32-entry stacks, and skipping
  * a subtree would change which pushes are dropped).  Mode 1 is that rule; two unsound
  * variants are kept so that tests can show what the rule's parts prevent: mode 2 leaves
- * out the loop restore, mode 3 prunes trees of any depth.  Process-wide. */
+ * out the loop restore, mode 3 prunes trees of any depth.  Mode 4 is a finer rule not yet
+ * in the engine: one largest-clear tmin per region of ORC_LIVE_REGION groups, and a loop
+ * re-enables the looped child's groups only in regions cleared above its new tmin.
+ * Process-wide. */
 #define ORC_LIVE_GROUPS 1024
 static int orc_live_mode;
 static int* orc_live_lo;
 static int* orc_live_hi;
 static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_active;
-void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 3) ? mode : 0; }
+void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 4) ? mode : 0; }
 
 /* Leaf ranges (first and last primitive in preorder) of every node, and the group
  * shift, for the tree about to be rendered. */
@@ -547,7 +550,12 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
     return 0;
 }
 
-typedef struct { uint64_t w[ORC_LIVE_GROUPS / 64]; double tclr; } orc_live;
+#define ORC_LIVE_REGION 128 /* groups per region: four 32-bit mask words */
+typedef struct {
+    uint64_t w[ORC_LIVE_GROUPS / 64];
+    double tclr;                               /* largest tmin of a traversal clear */
+    double treg[ORC_LIVE_GROUPS / ORC_LIVE_REGION]; /* the same per region (mode 4) */
+} orc_live;
 static int orc_live_any(const orc_live* m, int lo, int hi)
 {
     for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g)
@@ -559,13 +567,21 @@ static void orc_live_clear(orc_live* m, int lo, int hi, double tmin)
     const int sh = orc_live_shift;
     const int ga = (lo + (1 << sh) - 1) >> sh, gb = ((hi + 1) >> sh) - 1;
     if (ga > gb) return;
-    for (int g = ga; g <= gb; ++g) m->w[g >> 6] &= ~(1ull << (g & 63));
     const double tc = (tmin == tmin) ? tmin : INFINITY;
+    for (int g = ga; g <= gb; ++g) {
+        m->w[g >> 6] &= ~(1ull << (g & 63));
+        if (tc > m->treg[g / ORC_LIVE_REGION]) m->treg[g / ORC_LIVE_REGION] = tc;
+    }
     if (tc > m->tclr) m->tclr = tc;
 }
-static void orc_live_restore(orc_live* m, int lo, int hi)
+/* A loop to tmin re-enters the subtree with leaves [lo, hi]: mode 1 re-enables all its
+ * groups when tmin is below the ray's largest clear tmin, mode 4 those of the regions
+ * cleared above tmin. */
+static void orc_live_restore(orc_live* m, int lo, int hi, double tmin)
 {
-    for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g) m->w[g >> 6] |= 1ull << (g & 63);
+    if (orc_live_mode != 4 && tmin >= m->tclr) return;
+    for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g)
+        if (orc_live_mode != 4 || !(tmin >= m->treg[g / ORC_LIVE_REGION])) m->w[g >> 6] |= 1ull << (g & 63);
 }
 
 #define ORC_FMA 0

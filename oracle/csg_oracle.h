@@ -125,7 +125,8 @@ void orc_set_short_circuit(int on);
 
 /* Optional live-leaf pruning of the traversal (0 off, the default; 1 the engine's rule;
  * 2 the same without its loop restore and 3 the same on trees of any depth, both
- * unsound): see csg_oracle.c.  Process-wide. */
+ * unsound; 4 the rule with per-region restore records): see csg_oracle.c.
+ * Process-wide. */
 void orc_set_live_pruning(int mode);
 
 #ifdef __cplusplus

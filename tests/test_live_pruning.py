@@ -82,6 +82,8 @@ def test_live_pruning_keeps_every_plane(csg, oracle):
             got = _render(oracle, nodes, prims, cam, light, 40, 30, 1, sc)
             assert ref["capped"] == 0 and got["capped"] == 0
             assert _differ(ref, got) == 0, (i, sc)
+            fine = _render(oracle, nodes, prims, cam, light, 40, 30, 4, sc)  # per-region records
+            assert _differ(ref, fine) == 0, (i, sc)
             iters[0] += int(ref["counts"]["iters"].sum())
             iters[1] += int(got["counts"]["iters"].sum())
     assert iters[1] < 0.9 * iters[0]  # the rule skips work
@@ -97,6 +99,7 @@ def test_live_pruning_reentry_case(csg, oracle):
     for sc in (False, True):
         ref = _render(oracle, nodes, prims, cam, light, 48, 36, 0, sc)
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 1, sc)) == 0
+        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 4, sc)) == 0
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 2, sc)) > 0
 
 
@@ -148,3 +151,30 @@ def test_live_pruning_with_non_finite_parameters(csg, oracle):
         rendered += 1
         nan_hits += int(np.isnan(ref["t"][ref["hit"] != 0]).sum())
     assert rendered >= 40 and nan_hits > 0
+
+
+def test_region_records_restore_less_on_the_cheese_frame(csg, oracle):
+    """On the 3840x2160 cheese frame (every 16th pixel each way) one restore record per
+    ray re-enables whole subtrees that held no stale bit; per-region records (mode 4)
+    re-enable far less, with the same planes."""
+    from csgrt import scenes
+    text = scenes.config_scene_text(2, 0)
+    view = scenes.config_views(2, 0)[0]
+    nodes, prims = oracle.parse(text)
+    ys = np.arange(8, view.h, 16)
+    xs = np.arange(8, view.w, 16)
+    pix = (ys[:, None] * view.w + xs[None, :]).ravel()
+    out = {}
+    for mode in (0, 1, 2, 4):
+        oracle.set_live_pruning(mode)
+        try:
+            out[mode] = oracle.render_list(nodes, prims, view.camera, view.light, view.w, view.h, pix,
+                                           mode="fma", want=("t", "prim"), counts=True)
+        finally:
+            oracle.set_live_pruning(0)
+    for mode in (1, 2, 4):
+        assert np.array_equal(out[mode]["t"].view(np.uint32), out[0]["t"].view(np.uint32))
+        assert np.array_equal(out[mode]["prim"], out[0]["prim"])
+    it = {m: int(out[m]["counts"]["iters"].sum()) for m in out}
+    assert it[2] <= it[4] < it[1] < it[0]
+    assert it[4] < 1.02 * it[2] and it[1] > 1.1 * it[2]
