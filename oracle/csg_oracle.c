@@ -490,7 +490,9 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * traversal on the CPU.  Each ray starts with a mask over leaf groups (one bit per
  * 2^shift leaves in preorder, at most ORC_LIVE_GROUPS groups) holding the leaves whose
  * own box passes at tmin = 0 and whose primitive test at tmin = 0 is not a Miss (a cube:
- * its box alone).  GoTo treats a child without a live leaf as a Miss without testing it;
+ * its box alone); trees of fewer than ORC_LIVE_MIN_PRIMS primitives start all live, as
+ * the engine runs no pre-pass for them (a root leaf is tested without its box, and a
+ * cylinder's box does not contain the cylinder).  GoTo treats a child without a live leaf as a Miss without testing it;
  * a culled operator child clears the groups inside its leaf range and a leaf that returns
  * Miss its own bit (single-leaf groups only), recording the largest tmin of such a clear;
  * a loop whose new tmin is below that tmin marks the looped child's groups live again.
@@ -503,10 +505,11 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * re-enables the looped child's groups only in regions cleared above its new tmin.
  * Process-wide. */
 #define ORC_LIVE_GROUPS 1024
+#define ORC_LIVE_MIN_PRIMS 8
 static int orc_live_mode;
 static int* orc_live_lo;
 static int* orc_live_hi;
-static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_active;
+static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_prims, orc_live_active;
 void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 4) ? mode : 0; }
 
 /* Leaf ranges (first and last primitive in preorder) of every node, and the group
@@ -536,6 +539,7 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
     while (((n_prims + (1 << sh) - 1) >> sh) > ORC_LIVE_GROUPS) ++sh;
     orc_live_shift = sh;
     orc_live_nodes = n_nodes;
+    orc_live_prims = n_prims;
     /* operator depth: operators on the longest root-to-leaf path (parents precede
      * their children in preorder) */
     int depth = 0;

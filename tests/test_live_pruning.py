@@ -178,3 +178,20 @@ def test_region_records_restore_less_on_the_cheese_frame(csg, oracle):
     it = {m: int(out[m]["counts"]["iters"].sum()) for m in out}
     assert it[2] <= it[4] < it[1] < it[0]
     assert it[4] < 1.02 * it[2] and it[1] > 1.1 * it[2]
+
+
+def test_single_cylinder_root(csg, oracle):
+    """A root leaf is tested without its box, and a cylinder's box (BVHNode.cuh:34-49)
+    does not contain the cylinder: here a quarter of the hits lie outside it.  Trees this
+    small start all live (no pre-pass), so the rule keeps every one of them."""
+    text = "Cylinder 0 0 0 FF0000 0.6 1.6 30 20 10"
+    nodes, prims = oracle.parse(text)
+    d = np.array([0.2, 0.3, 1.0])
+    cam = csg.Camera.look_at_origin(d / np.linalg.norm(d), 3.0).floats()
+    light = np.float32(csg.light_dir())
+    ref = _render(oracle, nodes, prims, cam, light, 96, 72, 0, False)
+    pos = oracle.render(nodes, prims, cam, light, 96, 72, mode="fma", want=("hit", "pos"))
+    outside = (np.abs(pos["pos"][pos["hit"] != 0]) > 0.8).any(axis=1).sum()
+    assert outside > 100
+    for mode in (1, 4):
+        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 96, 72, mode, False)) == 0
