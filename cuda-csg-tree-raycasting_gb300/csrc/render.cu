@@ -5,7 +5,8 @@
 // reference round-trips a 36-byte RayHit per pixel); the only HBM traffic is the output
 // planes.  Each ray first finds the primitives it can hit at all (liveness pre-pass over
 // a BVH of the leaves), then runs the reference's traversal, skipping subtrees with no
-// live primitive left.
+// live primitive left (trees of up to 15 operator levels; deeper ones, whose stacks can
+// overflow, traverse every subtree as the reference does).
 #include <atomic>
 
 #include "pixel.cuh"
