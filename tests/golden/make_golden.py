@@ -22,6 +22,7 @@ from __future__ import annotations
 
 import json
 import math
+import os
 import shutil
 import sys
 from pathlib import Path
@@ -33,7 +34,9 @@ ROOT = GOLDEN.parent.parent
 sys.path.insert(0, str(ROOT))
 sys.path.insert(0, str(ROOT / "cuda-csg-tree-raycasting_gb300"))
 
-REF_TEST_DIR = Path("/root/reference/Test")
+# The reference checkout: CSG_REFERENCE_ROOT, as oracle/build_ref.py reads it.
+REF_ROOT = Path(os.environ.get("CSG_REFERENCE_ROOT", "/root/reference"))
+REF_TEST_DIR = REF_ROOT / "Test"
 FIX_W, FIX_H = 64, 48
 
 # Malformed inputs covering every error path of CSGTree::Parse (CSGTree.cu:24, 68, 91,
