@@ -13,16 +13,17 @@ constexpr int kThreads = 128;  // 4 warps per block: the single-view kernel, the
 
 // Shared memory of an nt-thread block: the per-ray primitive and time stacks (SD slots;
 // none when the stacks are in local memory), the per-ray live masks (live_words words)
-// and one BVH stack per warp.
+// with their restore records (one float per region of dev::kLiveRegionWords words) and
+// one BVH stack per warp.
 inline size_t smem_bytes(int sd, int live_words, int nt = kThreads, bool local_stacks = false)
 {
     return (local_stacks ? 0 : (size_t)sd * nt * 12) + (size_t)live_words * nt * 4 +
-           (size_t)(nt / 32) * dev::kWarpStack * 4;
+           (size_t)dev::live_regions(live_words) * nt * 4 + (size_t)(nt / 32) * dev::kWarpStack * 4;
 }
 
 struct BlockSmem {
     int* wstack;    // this warp's BVH stack
-    uint32_t* live; // live-mask base (word k of thread t at live[k * nt + t])
+    uint32_t* live; // live-mask base (word k of thread t at live[k * nt + t], then the restore records)
     int nt;         // threads per block
 };
 
@@ -52,7 +53,8 @@ __device__ __forceinline__ BlockSmem block_smem(unsigned char* smem_raw, int liv
 {
     BlockSmem b;
     b.live = reinterpret_cast<uint32_t*>(smem_raw + (LOCAL ? 0 : (size_t)SD * NT * 12));
-    b.wstack = reinterpret_cast<int*>(b.live + (size_t)live_words_alloc * NT) + (threadIdx.x >> 5) * dev::kWarpStack;
+    b.wstack = reinterpret_cast<int*>(b.live + (size_t)(live_words_alloc + dev::live_regions(live_words_alloc)) * NT) +
+               (threadIdx.x >> 5) * dev::kWarpStack;
     b.nt = NT;
     return b;
 }
@@ -92,7 +94,8 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
 // One pixel.  Must be called by all 32 lanes of a warp (the pre-pass walks the BVH
 // warp-cooperatively); lanes with inside == false only follow the walk.
 // FINE: the scene's fine live mask (single-view renders of large trees) instead of its own.
-template <int SD, bool ROLLED, bool FINE = false, class Stacks>
+// SCU: the unrolled traversal with the operator short-circuit (no effect on rolled ones).
+template <int SD, bool ROLLED, bool FINE = false, bool SCU = false, class Stacks>
 __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long long* status, uint32_t iter_cap,
                                              int x, int y, bool inside, Stacks& st, const BlockSmem& bs,
                                              const uint16_t* tab, dev::RayFrame frame)
@@ -108,7 +111,7 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     if constexpr (dev::kPrune<SD>) dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
     bool capped = false;
-    const dev::Hit h = dev::csg_traverse<SD, ROLLED>(p.scene, ray, st, tab, lm, iter_cap, &capped);
+    const dev::Hit h = dev::csg_traverse<SD, ROLLED, SCU>(p.scene, ray, st, tab, lm, iter_cap, &capped);
     write_pixel(p, status, ray, h, capped, x, y);
 }
 

@@ -61,7 +61,8 @@ struct RenderParams {
 
 // FINE: the scene's fine live mask (scenes with scene.fine set; rolled variants only).
 // LOCAL: the per-ray stacks in local memory (rolled scenes with large live masks).
-template <int SD, bool ROLLED, bool FINE, bool LOCAL>
+// SCU: the operator short-circuit in the unrolled variant (scenes with short_circuit set).
+template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU>
 __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG_UNROLLED_MIN_BLOCKS)
     render_tiled(const RenderParams p)
 {
@@ -79,11 +80,11 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     const int x = blockIdx.x * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
     const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
-    pix::render_pixel<SD, ROLLED, FINE>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st, bs,
-                                        tab, frame);
+    pix::render_pixel<SD, ROLLED, FINE, SCU>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st,
+                                             bs, tab, frame);
 }
 
-template <int SD, bool ROLLED, bool FINE, bool LOCAL>
+template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU = false>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
     const int words = FINE ? p.view.scene.fine_words : p.view.scene.live_words;
@@ -97,7 +98,7 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
     if (e != cudaSuccess) return e;
     const unsigned long long bit = device < 64 ? 1ull << device : 0ull;
     if (!(attr_set.load(std::memory_order_acquire) & bit) || !bit) {
-        const auto kernel = render_tiled<SD, ROLLED, FINE, LOCAL>;
+        const auto kernel = render_tiled<SD, ROLLED, FINE, LOCAL, SCU>;
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)pix::smem_bytes(SD, FINE ? kFineWordsMax : kLiveWordsMax, kThreads, LOCAL));
         if (e == cudaSuccess && CSG_TILED_CARVEOUT >= 0)
@@ -106,14 +107,17 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
         attr_set.fetch_or(bit, std::memory_order_release);
     }
     const dim3 grid((p.view.w + kTileW - 1) / kTileW, (p.view.h + kTileH - 1) / kTileH);
-    render_tiled<SD, ROLLED, FINE, LOCAL><<<grid, kThreads, smem, stream>>>(p);
+    render_tiled<SD, ROLLED, FINE, LOCAL, SCU><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 
 template <int SD>
 cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
 {
-    if (!p.view.scene.rolled) return launch_variant<SD, false, false, false>(p, stream);
+    if (!p.view.scene.rolled) {
+        if (SD < 32 && p.view.scene.short_circuit) return launch_variant<SD, false, false, false, true>(p, stream);
+        return launch_variant<SD, false, false, false>(p, stream);
+    }
     if (p.view.scene.fine) return launch_variant<SD, true, true, false>(p, stream);
     if (CSG_TILED_LOCAL_WORDS >= 0 && p.view.scene.live_words >= CSG_TILED_LOCAL_WORDS)
         return launch_variant<SD, true, false, true>(p, stream);

@@ -341,7 +341,6 @@ bool use_rolled(const HostTree& tree)
 
 bool use_short_circuit(const HostTree& tree)
 {
-    if (!use_rolled(tree)) return false;
     size_t ops = 0, decisive = 0;
     for (const RefNode& n : tree.nodes) {
         if (n.prim != -1) continue;
@@ -520,6 +519,15 @@ void pack_scene(const HostTree& t, PackedScene& out)
     for (size_t i = 0; i < n; ++i)
         if (num[i] < 0) num[i] = next++;
     auto dev = [&](int32_t old) { return old < 0 ? old : num[old]; };
+    // Traversal order of Intersections: Kensler's Intersection table (RaycastingKernels.cu:
+    // 670-673) is symmetric in its two children, ties included, so the device tree may
+    // list them in either order with the same results (leaf ranges stay contiguous, so the
+    // live mask and the primitive numbers are unchanged).  With the operator short-circuit
+    // a Miss from the child traversed first skips the other, so an Intersection of two
+    // operators puts the child with fewer leaves first: 20% fewer iterations on the
+    // batched workload's random trees (oracle, live-leaf pruning and short-circuit on).
+    const bool reorder = use_short_circuit(t) && t.op_depth <= 15;
+    auto n_leaves = [&](int32_t i) { return t.leaf_hi[i] - t.leaf_lo[i] + 1; };
     out.topo.assign(n, int4{0, 0, 0, 0});
     out.kids.assign(kKidsPerNode * std::max<size_t>(n_ops, 1), float4{0, 0, 0, 0});
     out.geo.assign(2 * np, float4{0, 0, 0, 0});
@@ -530,9 +538,13 @@ void pack_scene(const HostTree& t, PackedScene& out)
             out.topo[num[i]] = int4{nd.prim, -1, dev(nd.parent), nd.type};
             continue;
         }
-        out.topo[num[i]] = int4{dev(nd.left), dev(nd.right), dev(nd.parent), nd.type};
-        const RefNode& l = t.nodes[nd.left];
-        const RefNode& r = t.nodes[nd.right];
+        int32_t li = nd.left, ri = nd.right;
+        if (reorder && nd.type == kIntersection && t.nodes[li].prim == -1 && t.nodes[ri].prim == -1 &&
+            n_leaves(ri) < n_leaves(li))
+            std::swap(li, ri);
+        out.topo[num[i]] = int4{dev(li), dev(ri), dev(nd.parent), nd.type};
+        const RefNode& l = t.nodes[li];
+        const RefNode& r = t.nodes[ri];
         float4* k = &out.kids[kKidsPerNode * num[i]];
         k[0] = float4{l.minx, l.miny, l.minz, as_float(l.type)};
         k[1] = float4{l.maxx, l.maxy, l.maxz, as_float(l.prim)};
@@ -544,8 +556,8 @@ void pack_scene(const HostTree& t, PackedScene& out)
         // independent: disjoint leaf ranges, separate hit records).
         auto prio = [](const RefNode& c) { return c.prim == -1 ? 0 : c.type == kSphere ? 1 : c.type == kCube ? 2 : 3; };
         const int32_t swap = prio(r) < prio(l) ? (1 << 30) : 0;
-        k[4] = float4{as_float(t.leaf_lo[nd.left] | swap), as_float(t.leaf_hi[nd.left]), as_float(t.leaf_lo[nd.right]),
-                      as_float(t.leaf_hi[nd.right])};
+        k[4] = float4{as_float(t.leaf_lo[li] | swap), as_float(t.leaf_hi[li]), as_float(t.leaf_lo[ri]),
+                      as_float(t.leaf_hi[ri])};
     }
     // live-mask granularity: one bit per 2^shift leaves, at most kLiveWordsMax words
     int32_t shift = 0;

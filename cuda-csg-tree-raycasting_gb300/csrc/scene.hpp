@@ -151,10 +151,11 @@ bool use_prepass(int32_t n_prims);
 bool use_rolled(const HostTree& tree);
 
 // Whether the traversal short-circuits Difference and Intersection nodes decided by a Miss
-// child (trace.cuh): for trees of the rolled variant of which at least one operator in eight
-// is a Difference or an Intersection.  Measured: 2.2-6x faster on random trees; on the
-// cheese scene (one Difference over a 511-node Union, unrolled variant) the extra tests in
-// every GoTo cost 3-5% and saved nothing, so such trees keep the plain traversal.
+// child (trace.cuh): for trees of which at least one operator in eight is a Difference or
+// an Intersection.  Measured: 2.2-6x faster on random trees; on the cheese scene (one
+// Difference over a 511-node Union) the extra tests in every GoTo cost 3-5% and saved
+// nothing, so such trees keep the plain traversal.  The single-view kernel short-circuits
+// in both GoTo variants; the batched view-table kernel only in the rolled one.
 bool use_short_circuit(const HostTree& tree);
 
 // Whether a packed tree can use the fine live mask (rolled variant, grouped own mask, one

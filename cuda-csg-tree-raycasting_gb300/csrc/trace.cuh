@@ -537,14 +537,22 @@ struct LocalStacks {
 // child's t, which can lie below a tmin its other child's subtree has already looped to,
 // and a loop of an ancestor then re-enters that subtree with the lower tmin (the
 // reference does this on about one ray in several hundred of random trees).  Subtrees
-// are re-entered only through loops, so `tclr` keeps the largest tmin of any traversal
-// clear, and a loop whose new tmin is below it marks the looped child's leaves live again
-// (restore_range), which only prunes less.  A subtree whose leaves are all Miss
+// are re-entered only through loops, so each region of kLiveRegionWords mask words keeps
+// the largest tmin at which the traversal cleared one of its live bits (`region`), and a
+// loop whose new tmin is below a region's record marks the looped child's leaves in that
+// region live again (restore_range), which only prunes less; `tclr`, the largest record
+// of the ray, lets loops at or above every record skip the test.  One record per ray
+// re-enabled whole subtrees that held no stale bit: on the 3840x2160 cheese frame the
+// slowest rays then took 2.7x the iterations of the rule without the restore, and the
+// warps holding them ran for most of the launch.  A subtree whose leaves are all Miss
 // evaluates to a Miss whether or not it is traversed, and a Miss's t and index reach no
 // decision and no output, so skipping such a subtree changes nothing.  The mask lives in
-// shared memory, word k of a lane at w[k * nt]; `sum` has bit k set while word k is
-// non-zero (SumT: 32 bits for masks of up to 32 words, 64 bits for up to 64).
+// shared memory, word k of a lane at w[k * nt] and the record of region r right after the
+// words, at w[(words + r) * nt] (as a float); `sum` has bit k set while word k is non-zero
+// (SumT: 32 bits for masks of up to 32 words, 64 bits for up to 64).
 using live_sum_t = std::conditional<(kLiveWordsMax > 32), unsigned long long, uint32_t>::type;
+constexpr int kLiveRegionWords = 4;
+__host__ __device__ constexpr int live_regions(int words) { return (words + kLiveRegionWords - 1) / kLiveRegionWords; }
 
 template <typename SumT>
 struct LiveMaskT {
@@ -557,6 +565,16 @@ struct LiveMaskT {
     float tclr;  // largest tmin of a clear made during the traversal (-inf: none)
 
     __device__ __forceinline__ uint32_t& word(int k) { return w[k * nt]; }
+    __device__ __forceinline__ float& region(int k)
+    {
+        return reinterpret_cast<float*>(w)[(words + k / kLiveRegionWords) * nt];
+    }
+    // No clear recorded yet (before the traversal starts).
+    __device__ __forceinline__ void reset_records()
+    {
+        tclr = -INFINITY;
+        for (int r = 0; r < live_regions(words); ++r) region(r * kLiveRegionWords) = -INFINITY;
+    }
     __device__ __forceinline__ void fill(int n_groups)
     {
         sum = 0;
@@ -590,40 +608,46 @@ struct LiveMaskT {
         if (((sum >> wa) & 1u) && (word(wa) & ma)) return true;
         return ((sum >> wb) & 1u) && (word(wb) & mb);
     }
-    __device__ __forceinline__ void clear_word(int k, uint32_t m)
+    // Clears the bits m of word k at tmin tc (a NaN tmin counts as +inf: a loop to any
+    // tmin then restores the region).  Only bits that were live raise the records: a bit
+    // that was already clear keeps the validity of its earlier clear.
+    __device__ __forceinline__ void clear_word(int k, uint32_t m, float tc)
     {
-        const uint32_t v = word(k) & ~m;
+        const uint32_t old = word(k), v = old & ~m;
+        if (v == old) return;
         word(k) = v;
         if (!v) sum &= ~((live_sum_t)1 << k);
+        float& r = region(k);
+        r = fmaxf(r, tc);
+        tclr = fmaxf(tclr, tc);
     }
     __device__ __forceinline__ void clear_leaf(int leaf, float tmin)
     {
-        if (shift == 0) {
-            clear_word(leaf >> 5, 1u << (leaf & 31));
-            tclr = fmaxf(tclr, tmin == tmin ? tmin : INFINITY);
-        }
+        if (shift == 0) clear_word(leaf >> 5, 1u << (leaf & 31), tmin == tmin ? tmin : INFINITY);
     }
     // Clears the groups lying entirely inside [lo, hi].
     __device__ __forceinline__ void clear_range(int lo, int hi, float tmin)
     {
         const int ga = (lo + (1 << shift) - 1) >> shift, gb = ((hi + 1) >> shift) - 1;
         if (ga > gb) return;
-        tclr = fmaxf(tclr, tmin == tmin ? tmin : INFINITY);  // a NaN tmin: restore at every loop
+        const float tc = tmin == tmin ? tmin : INFINITY;
         const int wa = ga >> 5, wb = gb >> 5;
         for (int k = wa; k <= wb; ++k) {
             if (!((sum >> k) & 1u)) continue;
             const uint32_t lo_m = (k == wa) ? (0xffffffffu << (ga & 31)) : 0xffffffffu;
             const uint32_t hi_m = (k == wb) ? (0xffffffffu >> (31 - (gb & 31))) : 0xffffffffu;
-            clear_word(k, lo_m & hi_m);
+            clear_word(k, lo_m & hi_m, tc);
         }
     }
-    // Sets every group that holds a leaf of [lo, hi] (groups reaching outside the range
-    // too: more live bits only prune less).
-    __device__ __forceinline__ void restore_range(int lo, int hi)
+    // A loop to tmin re-enters the subtree with leaves [lo, hi]: sets every group that
+    // holds one of its leaves (groups reaching outside the range too: more live bits only
+    // prune less) in the words whose region recorded a clear above tmin.
+    __device__ __forceinline__ void restore_range(int lo, int hi, float tmin)
     {
         const int ga = lo >> shift, gb = hi >> shift;
         const int wa = ga >> 5, wb = gb >> 5;
         for (int k = wa; k <= wb; ++k) {
+            if (tmin >= region(k)) continue;
             const uint32_t lo_m = (k == wa) ? (0xffffffffu << (ga & 31)) : 0xffffffffu;
             const uint32_t hi_m = (k == wb) ? (0xffffffffu >> (31 - (gb & 31))) : 0xffffffffu;
             word(k) |= lo_m & hi_m;
@@ -671,7 +695,7 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
                                              int* wstack)
 {
     const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
-    lm.tclr = -INFINITY;
+    lm.reset_records();
     if (!sc.prepass || sc.n_bvh == 0) {
         lm.fill(n_groups);
         return;
@@ -843,13 +867,15 @@ template <int SD>
 constexpr bool kPrune = SD < 32;
 
 // A loop re-enters one child of operator `node` with a tmin below that of a traversal
-// clear: its leaves become live again (the leaf ranges are the node's kids record).
+// clear: its leaves in the regions cleared above tmin become live again (the leaf ranges
+// are the node's kids record).
 template <class LM>
-__device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restrict__ kids, int node, bool right)
+__device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restrict__ kids, int node, bool right,
+                                                   float tmin)
 {
     const int4 rg = __ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * node + 4]));
-    if (right) lm.restore_range(rg.z, rg.w);
-    else lm.restore_range(rg.x & 0x3fffffff, rg.y);
+    if (right) lm.restore_range(rg.z, rg.w, tmin);
+    else lm.restore_range(rg.x & 0x3fffffff, rg.y, tmin);
 }
 
 // Operator short-circuit (a tuning knob; 1 on).  Kensler's tables give Miss for a
@@ -861,9 +887,11 @@ __device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restr
 // skipped traversal would leave them (it pushes and pops in pairs when no stack can
 // overflow, SD < 32; the 32-entry class reproduces the reference's overflow behaviour, so it
 // always traverses).  Skipped subtrees keep their live bits, which only prunes less.
-// Rolled scenes opt in (DeviceScene::short_circuit, chosen by the scene compiler); the
-// unrolled variant, which serves small trees and sphere/cube scenes such as the cheese
-// frame, has no short-circuit code (with it, 3-5% slower there); 0 here removes it.
+// Scenes opt in (DeviceScene::short_circuit, chosen by the scene compiler).  The rolled
+// variant carries the code always; the unrolled variant, which serves small trees and
+// sphere/cube scenes such as the cheese frame, carries it only when instantiated with SCU
+// (with it, the cheese frame, which never short-circuits, was 3-5% slower).  0 here
+// removes it.
 #ifndef CSG_SHORT_CIRCUIT
 #define CSG_SHORT_CIRCUIT 1
 #endif
@@ -874,11 +902,12 @@ constexpr bool kShortCircuit = CSG_SHORT_CIRCUIT != 0;
 // ROLLED evaluates GoTo's tests (both children of an operator, or the leaf GoTo landed on)
 // in one rolled loop, so the primitive tests exist once in the code; the unrolled form
 // overlaps the two children's tests and is faster when the code stays small (scenes
-// without cylinders).
-template <int SD, bool ROLLED, class Stacks, class LM>
+// without cylinders).  SCU: the unrolled form with the operator short-circuit.
+template <int SD, bool ROLLED, bool SCU, class Stacks, class LM>
 __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Stacks& st,
                                             const uint16_t* tab, LM& lm)
 {
+    constexpr bool kSC = kShortCircuit && (ROLLED || SCU) && SD < 32;
     const int4* __restrict__ topo = sc.topo;
     const float4* __restrict__ kids = sc.kids;
     const float4* __restrict__ geo = sc.geo;
@@ -887,7 +916,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
     st.ntm = T.ntm;
     if (T.action & kSaveL) {
         T.tmin = st.tpop();
-        if (kShortCircuit && ROLLED && SD < 32 && sc.short_circuit && (T.L.hit & kMiss) &&
+        if (kSC && sc.short_circuit && (T.L.hit & kMiss) &&
             (T.ct.w == kDifference || T.ct.w == kIntersection)) {
             // The left subtree returned a Miss: the node's Compute gives Miss whatever the
             // right subtree returns, so it is not traversed (the pending LoadL is dropped;
@@ -962,7 +991,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             // child is such a Miss, or an Intersection with one, computes Miss whatever
             // the other child returns: go straight to Compute.
             const bool lmiss = !gl && (T.L.hit & kMiss), rmiss = !gr && (T.R.hit & kMiss);
-            const bool decided = kShortCircuit && ROLLED && SD < 32 && sc.short_circuit &&
+            const bool decided = kSC && sc.short_circuit &&
                                  ((T.ct.w == kDifference && lmiss) || (T.ct.w == kIntersection && (lmiss || rmiss)));
             if (decided) {
                 T.action = kCompute;
@@ -1014,13 +1043,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             tracer_parent(T, topo);
         } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
             T.tmin = T.L.t;
-            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false);
+            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false, T.tmin);
             st.ppush(T.R);
             T.as.push(kLoadR);
             T.action = kGotoL;
         } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
             T.tmin = T.R.t;
-            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true);
+            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true, T.tmin);
             st.ppush(T.L);
             T.as.push(kLoadL);
             T.action = kGotoR;
@@ -1037,7 +1066,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
 
 // Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
 // stopped at iter_cap; *capped is then set).
-template <int SD, bool ROLLED, class Stacks, class LM>
+template <int SD, bool ROLLED, bool SCU, class Stacks, class LM>
 __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, Stacks& st,
                                             const uint16_t* tab, LM& lm, uint32_t iter_cap, bool* capped)
 {
@@ -1049,7 +1078,7 @@ __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ra
             *capped = true;
             return hit_default();
         }
-        tracer_step<SD, ROLLED>(T, sc, st, tab, lm);
+        tracer_step<SD, ROLLED, SCU>(T, sc, st, tab, lm);
     }
     *capped = false;
     return T.L;

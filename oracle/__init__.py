@@ -71,6 +71,12 @@ class Oracle:
         L.orc_set_short_circuit.restype = None
         L.orc_set_live_pruning.argtypes = [_i]
         L.orc_set_live_pruning.restype = None
+        L.orc_set_live_region.argtypes = [_i]
+        L.orc_set_live_region.restype = None
+        L.orc_set_union_shortcut.argtypes = [_i]
+        L.orc_set_union_shortcut.restype = None
+        L.orc_set_leaf_shortcut.argtypes = [_i]
+        L.orc_set_leaf_shortcut.restype = None
         L.orc_boxes_exact.argtypes = [_vp, _i, _vp]
         L.orc_boxes_exact.restype = None
         L.orc_tan_half_fov.restype = _f
@@ -139,10 +145,26 @@ class Oracle:
 
     def set_live_pruning(self, mode: int):
         """The engine's live-leaf pruning in the traversal: 0 off (the reference's own),
-        1 the engine's rule, 2 the rule without its loop restore, 3 the rule on trees of
-        any depth (2 and 3 are unsound), 4 the rule with one restore record per region of
-        four mask words (not yet in the engine)."""
+        1 one restore record per ray, 2 the rule without its loop restore, 3 the rule on
+        trees of any depth (2 and 3 are unsound), 4 one restore record per region of
+        `set_live_region` groups, 5 and 6 modes 1 and 4 restoring only groups that were
+        live at tmin = 0."""
         self.lib.orc_set_live_pruning(int(mode))
+
+    def set_union_shortcut(self, max_leaves: int):
+        """With live-leaf pruning: an all-Union operator subtree of at most max_leaves
+        leaves with one live leaf is evaluated as that leaf (0: off)."""
+        self.lib.orc_set_union_shortcut(int(max_leaves))
+
+    def set_leaf_shortcut(self, max_leaves: int):
+        """With live-leaf pruning: any operator subtree of at most max_leaves leaves with
+        one live leaf evaluates to that leaf's result when the path down to it passes only
+        Unions and Differences entered on their left, else to a Miss (0: off)."""
+        self.lib.orc_set_leaf_shortcut(int(max_leaves))
+
+    def set_live_region(self, groups: int):
+        """Groups per restore record of pruning modes 4 and 6 (default 128: four mask words)."""
+        self.lib.orc_set_live_region(int(groups))
 
     def tan_half_fov(self, fov: float) -> float:
         return float(np.float32(self.lib.orc_tan_half_fov(fov)))

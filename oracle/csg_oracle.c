@@ -494,15 +494,17 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * the engine runs no pre-pass for them (a root leaf is tested without its box, and a
  * cylinder's box does not contain the cylinder).  GoTo treats a child without a live leaf as a Miss without testing it;
  * a culled operator child clears the groups inside its leaf range and a leaf that returns
- * Miss its own bit (single-leaf groups only), recording the largest tmin of such a clear;
- * a loop whose new tmin is below that tmin marks the looped child's groups live again.
- * The engine prunes only trees of at most 15 operator levels, whose stacks cannot
- * overflow (deeper trees keep the reference's drop-on-full 32-entry stacks, and skipping
- * a subtree would change which pushes are dropped).  Mode 1 is that rule; two unsound
- * variants are kept so that tests can show what the rule's parts prevent: mode 2 leaves
- * out the loop restore, mode 3 prunes trees of any depth.  Mode 4 is a finer rule not yet
- * in the engine: one largest-clear tmin per region of ORC_LIVE_REGION groups, and a loop
- * re-enables the looped child's groups only in regions cleared above its new tmin.
+ * Miss its own bit (single-leaf groups only), and each region of orc_live_region groups
+ * records the largest tmin at which one of its live groups was cleared; a loop re-enables
+ * the looped child's groups in the regions whose record is above its new tmin.  The
+ * engine prunes only trees of at most 15 operator levels, whose stacks cannot overflow
+ * (deeper trees keep the reference's drop-on-full 32-entry stacks, and skipping a subtree
+ * would change which pushes are dropped).  Mode 4 is that rule (the engine's regions are
+ * four 32-bit mask words, ORC_LIVE_REGION groups).  Mode 1 is the engine's earlier rule,
+ * one record per ray raised by every clear, which re-enables whole subtrees that held no
+ * stale group; modes 5 and 6 are modes 1 and 4 re-enabling only groups that were live at
+ * tmin = 0.  Two unsound variants are kept so that tests can show what the rule's parts
+ * prevent: mode 2 leaves out the loop restore, mode 3 prunes trees of any depth.
  * Process-wide. */
 #define ORC_LIVE_GROUPS 1024
 #define ORC_LIVE_MIN_PRIMS 8
@@ -510,7 +512,7 @@ static int orc_live_mode;
 static int* orc_live_lo;
 static int* orc_live_hi;
 static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_prims, orc_live_active;
-void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 4) ? mode : 0; }
+void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 6) ? mode : 0; }
 
 /* Leaf ranges (first and last primitive in preorder) of every node, and the group
  * shift, for the tree about to be rendered. */
@@ -527,12 +529,15 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
         orc_live_hi = hi;
         orc_live_cap = n_nodes;
     }
+    /* (min and max over both children: a tree whose operators' children were swapped, as
+     * the engine may do for Intersections, keeps every subtree's leaves contiguous) */
     for (int i = n_nodes - 1; i >= 0; --i) {
         if (nodes[i].prim != -1) {
             orc_live_lo[i] = orc_live_hi[i] = nodes[i].prim;
         } else {
-            orc_live_lo[i] = orc_live_lo[nodes[i].left];
-            orc_live_hi[i] = orc_live_hi[nodes[i].right];
+            const int a = nodes[i].left, b = nodes[i].right;
+            orc_live_lo[i] = orc_live_lo[a] < orc_live_lo[b] ? orc_live_lo[a] : orc_live_lo[b];
+            orc_live_hi[i] = orc_live_hi[a] > orc_live_hi[b] ? orc_live_hi[a] : orc_live_hi[b];
         }
     }
     int sh = 0;
@@ -554,11 +559,74 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
     return 0;
 }
 
+/* Single-leaf shortcut (a candidate engine rule, with live-leaf pruning, off by default):
+ * an operator subtree of at most orc_shortcut_max leaves, one bit per leaf, with exactly
+ * one live leaf l evaluates without descending.  Every other leaf of it is a Miss, and
+ * by Kensler's tables (RaycastingKernels.cu:666-677) a Union with a Miss child returns
+ * the other child's record, a Difference returns its left child's record when the right
+ * one is a Miss and Miss when the left one is, and an Intersection with a Miss child
+ * returns Miss (a Miss's t and index reach no decision).  So the subtree's result is l's
+ * own result (tested with its box, which every box on the path contains) when every
+ * operator on the path down to l is a Union or a Difference entered on its left, and a
+ * Miss otherwise.  orc_blk[l] is the depth of the deepest operator above l entered
+ * otherwise (-1: none), and the path below a node of depth d is transparent when
+ * orc_blk[l] < d.  Mode 1 of orc_set_union_shortcut allows only all-Union subtrees. */
+static int orc_shortcut_max, orc_shortcut_general;
+static int* orc_uonly;     /* per node: every operator of its subtree is a Union */
+static int* orc_depth;     /* per node: operators above it */
+static int* orc_leaf_node; /* per primitive: its node */
+static int* orc_blk;       /* per primitive: see above */
+static int orc_uonly_cap, orc_leaf_cap;
+void orc_set_union_shortcut(int max_leaves) { orc_shortcut_max = max_leaves > 0 ? max_leaves : 0; orc_shortcut_general = 0; }
+void orc_set_leaf_shortcut(int max_leaves) { orc_shortcut_max = max_leaves > 0 ? max_leaves : 0; orc_shortcut_general = 1; }
+static int orc_shortcut_prepare(const orc_node* nodes, int n_nodes, int n_prims)
+{
+    if (n_nodes > orc_uonly_cap) {
+        int* u = (int*)realloc(orc_uonly, sizeof(int) * (size_t)n_nodes);
+        if (!u) return -1;
+        orc_uonly = u;
+        int* d = (int*)realloc(orc_depth, sizeof(int) * (size_t)n_nodes);
+        if (!d) return -1;
+        orc_depth = d;
+        orc_uonly_cap = n_nodes;
+    }
+    if (n_prims > orc_leaf_cap) {
+        int* l = (int*)realloc(orc_leaf_node, sizeof(int) * (size_t)n_prims);
+        if (!l) return -1;
+        orc_leaf_node = l;
+        int* b = (int*)realloc(orc_blk, sizeof(int) * (size_t)n_prims);
+        if (!b) return -1;
+        orc_blk = b;
+        orc_leaf_cap = n_prims;
+    }
+    for (int i = n_nodes - 1; i >= 0; --i) {
+        if (nodes[i].prim != -1) {
+            orc_uonly[i] = 1;
+            if (nodes[i].prim >= 0 && nodes[i].prim < n_prims) orc_leaf_node[nodes[i].prim] = i;
+        } else {
+            orc_uonly[i] = nodes[i].type == ORC_UNION && orc_uonly[nodes[i].left] && orc_uonly[nodes[i].right];
+        }
+    }
+    for (int i = 0; i < n_nodes; ++i) orc_depth[i] = nodes[i].parent >= 0 ? orc_depth[nodes[i].parent] + 1 : 0;
+    for (int p = 0; p < n_prims; ++p) {
+        int blk = -1;
+        for (int c = orc_leaf_node[p], a = nodes[c].parent; a >= 0; c = a, a = nodes[a].parent) {
+            const int transparent = nodes[a].type == ORC_UNION || (nodes[a].type == ORC_DIFFERENCE && nodes[a].left == c);
+            if (!transparent) { blk = orc_depth[a]; break; }
+        }
+        orc_blk[p] = blk;
+    }
+    return 0;
+}
+
 #define ORC_LIVE_REGION 128 /* groups per region: four 32-bit mask words */
+static int orc_live_region = ORC_LIVE_REGION; /* groups per restore record (modes 4 and 6) */
+void orc_set_live_region(int groups) { orc_live_region = (groups >= 1 && groups <= ORC_LIVE_GROUPS) ? groups : ORC_LIVE_REGION; }
 typedef struct {
     uint64_t w[ORC_LIVE_GROUPS / 64];
+    uint64_t p[ORC_LIVE_GROUPS / 64];          /* the mask at tmin = 0 (modes 5 and 6) */
     double tclr;                               /* largest tmin of a traversal clear */
-    double treg[ORC_LIVE_GROUPS / ORC_LIVE_REGION]; /* the same per region (mode 4) */
+    double treg[ORC_LIVE_GROUPS];              /* the same per region (modes 4 and 6) */
 } orc_live;
 static int orc_live_any(const orc_live* m, int lo, int hi)
 {
@@ -566,26 +634,53 @@ static int orc_live_any(const orc_live* m, int lo, int hi)
         if ((m->w[g >> 6] >> (g & 63)) & 1u) return 1;
     return 0;
 }
+/* The single-leaf shortcut for operator `node` with leaves [lo, hi]: -1 when it does not
+ * apply; else the node of the subtree's one live leaf, with *miss set when the path down
+ * to it is not transparent (the subtree is then a Miss). */
+static int orc_shortcut_leaf(const orc_live* m, int node, int lo, int hi, int* miss)
+{
+    *miss = 0;
+    if (!orc_shortcut_max || orc_live_shift != 0 || hi - lo + 1 > orc_shortcut_max) return -1;
+    if (!orc_shortcut_general && !orc_uonly[node]) return -1;
+    int found = -1;
+    for (int g = lo; g <= hi; ++g)
+        if ((m->w[g >> 6] >> (g & 63)) & 1u) {
+            if (found >= 0) return -1;
+            found = g;
+        }
+    if (found < 0) return -1;
+    *miss = !(orc_blk[found] < orc_depth[node]);
+    return orc_leaf_node[found];
+}
 static void orc_live_clear(orc_live* m, int lo, int hi, double tmin)
 {
     const int sh = orc_live_shift;
     const int ga = (lo + (1 << sh) - 1) >> sh, gb = ((hi + 1) >> sh) - 1;
     if (ga > gb) return;
     const double tc = (tmin == tmin) ? tmin : INFINITY;
+    const int regional = (orc_live_mode == 4 || orc_live_mode == 6);
     for (int g = ga; g <= gb; ++g) {
-        m->w[g >> 6] &= ~(1ull << (g & 63));
-        if (tc > m->treg[g / ORC_LIVE_REGION]) m->treg[g / ORC_LIVE_REGION] = tc;
+        const uint64_t bit = 1ull << (g & 63);
+        /* per-region records are raised only by groups that were live (a group already
+         * clear keeps the validity of its earlier clear) */
+        if (regional && !(m->w[g >> 6] & bit)) continue;
+        m->w[g >> 6] &= ~bit;
+        if (tc > m->treg[g / orc_live_region]) m->treg[g / orc_live_region] = tc;
     }
     if (tc > m->tclr) m->tclr = tc;
 }
 /* A loop to tmin re-enters the subtree with leaves [lo, hi]: mode 1 re-enables all its
  * groups when tmin is below the ray's largest clear tmin, mode 4 those of the regions
- * cleared above tmin. */
+ * cleared above tmin; modes 5 and 6 are modes 1 and 4 re-enabling only groups that were
+ * live at tmin = 0 (a group the pre-pass cleared is a Miss at every tmin). */
 static void orc_live_restore(orc_live* m, int lo, int hi, double tmin)
 {
-    if (orc_live_mode != 4 && tmin >= m->tclr) return;
+    const int regional = (orc_live_mode == 4 || orc_live_mode == 6);
+    const int keep = (orc_live_mode == 5 || orc_live_mode == 6);
+    if (!regional && tmin >= m->tclr) return;
     for (int g = lo >> orc_live_shift; g <= (hi >> orc_live_shift); ++g)
-        if (orc_live_mode != 4 || !(tmin >= m->treg[g / ORC_LIVE_REGION])) m->w[g >> 6] |= 1ull << (g & 63);
+        if (!regional || !(tmin >= m->treg[g / orc_live_region]))
+            if (!keep || ((m->p[g >> 6] >> (g & 63)) & 1u)) m->w[g >> 6] |= 1ull << (g & 63);
 }
 
 #define ORC_FMA 0

@@ -123,11 +123,18 @@ int orc_render_list_fma(const orc_node* nodes, int n_nodes, const orc_prim* prim
  * algorithm): see csg_oracle.c.  Process-wide. */
 void orc_set_short_circuit(int on);
 
-/* Optional live-leaf pruning of the traversal (0 off, the default; 1 the engine's rule;
- * 2 the same without its loop restore and 3 the same on trees of any depth, both
- * unsound; 4 the rule with per-region restore records): see csg_oracle.c.
- * Process-wide. */
+/* Optional live-leaf pruning of the traversal (0 off, the default; 1 one restore record
+ * per ray; 2 the same without its loop restore and 3 the same on trees of any depth, both
+ * unsound; 4 one restore record per region of orc_set_live_region groups; 5 and 6 are
+ * 1 and 4 restoring only groups live at tmin = 0): see csg_oracle.c.  Process-wide. */
 void orc_set_live_pruning(int mode);
+void orc_set_live_region(int groups);
+/* Union shortcut (with live-leaf pruning; 0 off, the default): an all-Union operator
+ * subtree of at most max_leaves leaves with one live leaf is evaluated as that leaf. */
+void orc_set_union_shortcut(int max_leaves);
+/* The same for any operator subtree: its result is the live leaf's when every operator on
+ * the path down to it is a Union or a Difference entered on its left, else a Miss. */
+void orc_set_leaf_shortcut(int max_leaves);
 
 #ifdef __cplusplus
 }

@@ -46,7 +46,7 @@ def reorder(tree, order):
 
 def _render(oracle, text, cam, light, w, h, engine_rules):
     nodes, prims = oracle.parse(text)
-    oracle.set_live_pruning(1 if engine_rules else 0)
+    oracle.set_live_pruning(4 if engine_rules else 0)
     oracle.set_short_circuit(engine_rules)
     try:
         thf = oracle.tan_half_fov(float(cam[5]))
@@ -94,3 +94,54 @@ def test_intersection_children_commute(csg, oracle):
                 iters[1] += int(b["counts"]["iters"].sum())
     assert swapped_trees >= 50
     assert iters[1] < 0.95 * iters[0]  # 0.93 on this sample
+
+
+def engine_order(nodes):
+    """The scene compiler's Intersection order applied to a parsed node array: an
+    Intersection of two operators lists the child with fewer leaves first.  Leaves keep
+    their numbers (every subtree's leaves stay contiguous), so the planes, primitive
+    indices included, must not change."""
+    nodes = nodes.copy()
+    n = len(nodes)
+    leaves = np.zeros(n, np.int64)
+    for i in range(n - 1, -1, -1):
+        leaves[i] = 1 if nodes[i]["prim"] != -1 else leaves[nodes[i]["left"]] + leaves[nodes[i]["right"]]
+    swapped = 0
+    for i in range(n):
+        l, r = int(nodes[i]["left"]), int(nodes[i]["right"])
+        if nodes[i]["type"] == 2 and nodes[l]["prim"] == -1 and nodes[r]["prim"] == -1 and leaves[r] < leaves[l]:
+            nodes[i]["left"], nodes[i]["right"] = r, l
+            swapped += 1
+    return nodes, swapped
+
+
+def test_engine_order_keeps_every_plane(csg, oracle):
+    """The engine's rule on node arrays (children swapped in place, no renumbering): every
+    plane identical under the reference's traversal and under the engine's rules, and ~20%
+    fewer iterations with them on the batched workload's trees."""
+    from csgrt import scenes
+    light = np.float32(csg.light_dir())
+    work = scenes.config_batch(0, n_scenes=96)
+    iters = [0, 0]
+    swapped_trees = 0
+    for s, (text, views) in enumerate(work):
+        nodes, prims = oracle.parse(text)
+        nodes2, k = engine_order(nodes)
+        swapped_trees += k > 0
+        cam = views[0].camera
+        for rules in ((False, True) if s < 24 else (True,)):
+            outs = []
+            for nd in (nodes, nodes2):
+                oracle.set_live_pruning(4 if rules else 0)
+                oracle.set_short_circuit(rules)
+                try:
+                    outs.append(oracle.render(nd, prims, cam, light, 40, 30, mode="fma", want=PLANES, counts=True))
+                finally:
+                    oracle.set_live_pruning(0)
+                    oracle.set_short_circuit(False)
+            assert _same(outs[0], outs[1], np.arange(len(prims))), (s, rules)
+            if rules:
+                iters[0] += int(outs[0]["counts"]["iters"].sum())
+                iters[1] += int(outs[1]["counts"]["iters"].sum())
+    assert swapped_trees >= 20
+    assert iters[1] < 0.9 * iters[0]
