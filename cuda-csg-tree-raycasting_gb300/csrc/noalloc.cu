@@ -19,6 +19,12 @@
 // code is pix::render_pixel, shared with the single-view and batched kernels, so every
 // view's planes are the bytes csg_render_planes writes.
 //
+// One call renders all its views with one kernel variant: the largest stack class and
+// live mask of its views, and the rolled GoTo loop if any view's scene has it.  The planes
+// are the same whatever the variant, but a single tree deeper than 15 operator levels (the
+// 32-entry stack class, which traverses without live-leaf pruning) makes every view of the
+// call traverse without it, so callers should group views by tree class, as csg_batch does.
+//
 // Only the work counter must start at zero; every call's first fill launch clears it on
 // the call's stream, ahead of the render launch.  Rays stopped at the iteration cap are
 // counted in each view's scene, as csg_render_planes counts them, and csg_scene_check
@@ -51,8 +57,9 @@ static_assert(kPrefixOffset + sizeof(int32_t) * (kMaxViews + 1) <= kScratchBytes
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
-// One fill launch: up to kChunk view records and their tile prefixes, passed by value.
-constexpr int kChunk = 112;
+// One fill launch: up to kChunk view records and their tile prefixes, passed by value
+// (12 KB of the calling thread's stack; the whole call uses about 21 KB of it).
+constexpr int kChunk = 56;
 struct FillChunk {
     ViewRecord rec[kChunk];
     int32_t prefix[kChunk];
@@ -150,26 +157,26 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
     unsigned char* scratch = scratch_on(device);
     if (!scratch) return CSG_E_CUDA;
 
-    // Longest-first order and the tile prefix, in fixed-size stack buffers.
-    int32_t order[kMaxViews];
-    int32_t prefix[kMaxViews + 1];
-    for (int32_t i = 0; i < n_views; ++i) order[i] = i;
-    std::sort(order, order + n_views, [&](int32_t a, int32_t b) {
+    // Longest-first order (a fixed-size stack buffer of 16-bit view numbers) and the
+    // total of warp tiles, checked before anything is enqueued.
+    static_assert(kMaxViews <= 32768, "view numbers are 16-bit");
+    int16_t order[kMaxViews];
+    for (int32_t i = 0; i < n_views; ++i) order[i] = static_cast<int16_t>(i);
+    std::sort(order, order + n_views, [&](int16_t a, int16_t b) {
         const double ca = view_cost(views[a]), cb = view_cost(views[b]);
         return ca > cb || (ca == cb && a < b);
     });
     long long total = 0;
     for (int32_t k = 0; k < n_views; ++k) {
         const csg_view& v = views[order[k]];
-        prefix[k] = static_cast<int32_t>(total);
         total += view_tiles(v.w, v.h, tw);
         if (total > INT_MAX) return CSG_E_CAPACITY;
     }
-    prefix[n_views] = static_cast<int32_t>(total);
 
-    // View records and prefixes, by value through the fill launches' parameters.
+    // View records and tile prefixes, by value through the fill launches' parameters.
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     FillChunk c;
+    long long first_item = 0;
     for (int32_t k0 = 0; k0 < n_views; k0 += kChunk) {
         const int32_t n = std::min<int32_t>(kChunk, n_views - k0);
         for (int32_t j = 0; j < n; ++j) {
@@ -179,7 +186,8 @@ extern "C" int csg_render_views_noalloc(const csg_view* views, int32_t n_views, 
             const Planes out{dp.rgba8, reinterpret_cast<float4*>(dp.rgba32f), dp.t, dp.prim, dp.normal};
             make_view_record(v.scene->dev, v.scene->status, reinterpret_cast<const float*>(&v.cam), v.light_dir,
                              v.w, v.h, out, tw, c.rec[j]);
-            c.prefix[j] = prefix[k0 + j];
+            c.prefix[j] = static_cast<int32_t>(first_item);
+            first_item += view_tiles(v.w, v.h, tw);
         }
         c.k0 = k0;
         c.n = n;

@@ -248,10 +248,18 @@ int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
  * gives CSG_E_CAPACITY, and a view with pageable host planes CSG_E_ARG, before anything
  * is enqueued (planes may be device or page-locked host memory, as for csg_batch_create).
  * Asynchronous on `stream`; capped
- * rays are counted per scene (csg_scene_check).  The first call on a device does set-up
- * (looks up the array's address, sets kernel attributes): make it before any stream
- * capture on that device.  All calls on a device share the one array, so calls whose
- * work may overlap (different streams, unsynchronised threads) race: serialise them. */
+ * rays are counted per scene (csg_scene_check).  Set-up: the first call on a device looks
+ * up the array's address there, and the first call with each kernel variant (stack class,
+ * rolled GoTo loop, block shape) and live-mask size on a device sets that kernel's
+ * attributes and queries its occupancy (a fixed table of 64 such entries per variant; once
+ * it is full, new sizes redo the query on every call).  Make a call with every variant a
+ * capture will use before any stream capture on that device.  All calls on a device share
+ * the one array, so calls whose work may overlap (different streams, unsynchronised
+ * threads) race: serialise them.  One call renders all its views with one kernel variant,
+ * that of its heaviest view (largest stack class and live mask, rolled if any view is):
+ * the planes are the same, but one tree deeper than 15 operator levels turns live-leaf
+ * pruning off for every view of the call, so group views by tree class as csg_batch does.
+ * The call uses about 21 KB of the calling thread's stack. */
 #define CSG_NOALLOC_MAX_VIEWS 4096
 int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream);
 
