@@ -194,6 +194,44 @@ def traffic_from_profiles(kernel_key: str):
         return None
 
 
+def frame_speedup(config: int, steps: int = 10, warmup: int = 3, seed: int = 0):
+    """One configuration's frame through the engine (csg_render_planes, RGBA8 device plane,
+    L2 flushed before each step, CUDA events) and through the reference's own kernels on
+    the same GPU: a reduced measurement for the default run's summary."""
+    import torch
+    import csgrt
+    text, view = load_scene_and_view(config, seed)
+    w, h = view.w, view.h
+    scene = csgrt.Scene(text)
+    cam = csgrt.Camera.from_floats(view.camera)
+    stream = torch.cuda.current_stream()
+    out = torch.empty(w * h, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    for _ in range(warmup):
+        flush.zero_()
+        scene.render_ptrs(cam, view.light, w, h, rgba8=out.data_ptr(), stream=stream.cuda_stream)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        flush.zero_()
+        a.record(stream)
+        scene.render_ptrs(cam, view.light, w, h, rgba8=out.data_ptr(), stream=stream.cuda_stream)
+        b.record(stream)
+    torch.cuda.synchronize()
+    if scene.check(stream.cuda_stream) != 0:
+        raise RuntimeError("rays stopped at the traversal iteration cap")
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    info = scene.info()
+    scene.close()
+    res = {"workload": WORKLOADS[config], "seed": seed, "width": w, "height": h, "nodes": info["n_nodes"],
+           "kernel_ms": round(ms, 4), "value": round(w * h / (ms * 1e-3) / 1e6, 3), "unit": "Mrays/s",
+           "steps": steps, "warmup": warmup}
+    rc = reference_cuda(text, view)
+    if rc:
+        res["reference_cuda"] = {"value": round(rc["value"], 3), "ms_frame": round(rc["ms_frame"], 4)}
+        res["engine_speedup"] = round(res["value"] / rc["value"], 2)
+    return res
+
+
 def run_engine(args):
     import torch
     import csgrt
@@ -327,8 +365,11 @@ def run_engine(args):
         res["cpu_baseline"] = cpu_baseline(text, view, seconds=args.cpu_seconds)
     scene.close()
     if args.config == 2 and not args.no_extras:
-        # the metric's other two parts, on reduced runs: batched vs per-view launches
-        # (configuration 4) and request latency under load (configuration 5, 1,000 req/s)
+        # the other single-view configurations (1: the README tree, 3: a random tree) against
+        # the reference's kernels; then the metric's other two parts, on reduced runs:
+        # batched vs per-view launches (configuration 4) and request latency under load
+        # (configuration 5, 1,000 req/s)
+        res["other_frames"] = {f"config{c}": frame_speedup(c) for c in (1, 3)}
         sub = argparse.Namespace(**vars(args))
         sub.steps, sub.warmup, sub.no_reference_cuda = 2, 3, True
         b = run_batch(sub, sub=True)
@@ -426,6 +467,25 @@ def run_batch(args, sub=False):
     pv_steps = max(2, min(args.steps, 5))
     pv_ms = timed(per_view, pv_steps)
 
+    # per class: the class's views as per-view launches (one event pair around them), next
+    # to the class's own persistent launch timed alone by the autotuner
+    def class_key(sc):
+        i = sc.info()
+        b = 1
+        while b < i["live_words"]:
+            b <<= 1
+        return (i["stack_class"], int(i["rolled"]), b)
+
+    by_class = {}
+    for v in views:
+        by_class.setdefault(class_key(v[0]), []).append(v)
+    class_pv_ms = {}
+    for key, vs in by_class.items():
+        def pv_class(vs=vs):
+            for sc, cam, light, w, h, pl in vs:
+                sc.render_ptrs(cam, light, w, h, rgba8=pl["rgba8"], stream=stream.cuda_stream)
+        class_pv_ms[key] = float(np.median(timed(pv_class, 3)))
+
     # the reference's own kernels, one RaycastKernel + LightningKernel launch pair per view
     ref_pv = None
     if not args.no_reference_cuda:
@@ -503,7 +563,10 @@ def run_batch(args, sub=False):
                                "live_words": c["live_words"], "warp_tile": [c["warp_tile_w"], 32 // c["warp_tile_w"]],
                                "warps_per_block": c["warps_per_block"],
                                "stacks": "local" if c["local_stacks"] else "shared",
-                               "tuned_ms": round(c["tuned_ms"], 3)} for c in batch.classes()]},
+                               "tuned_ms": round(c["tuned_ms"], 3),
+                               "per_view_launches_ms": round(class_pv_ms.get(
+                                   (c["stack_class"], int(c["rolled"]), c["live_words"]), float("nan")), 3)}
+                              for c in batch.classes()]},
         "per_view_launches": {"value": round(pv_value, 3), "unit": "Mrays/s", "launches": len(views),
                               "ms_per_step": round(float(np.mean(pv_ms)), 3),
                               "note": "the same 1024 views, one csg_render_planes launch each, one stream"},
