@@ -380,6 +380,7 @@ def run_engine(args):
         srv = run_serving(sub, sub=True, rates=(1000,), n_req=512)
         row = srv["serving"][0]
         res["serving"] = {"workload": WORKLOADS[5], "rate_rps": 1000, "requests": row["requests"],
+                          "order": srv["config"]["order"],
                           "batched": {k: row["batched"][k] for k in ("p50_ms", "p99_ms", "mrays_s")},
                           "per_request": {k: row["per_request"][k] for k in ("p50_ms", "p99_ms", "mrays_s")}}
     print(json.dumps(res), flush=True)
@@ -612,7 +613,7 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=512):
     ws, rank, local = dist_info()
     torch.cuda.set_device(local)
     n_pool = 1024
-    srv = csgrt.Server(hbm_budget=40 << 30, slots=4, max_batch_views=256)
+    srv = csgrt.Server(hbm_budget=40 << 30, slots=8, max_batch_views=256, order=args.serve_order)
     t_setup = time.perf_counter()
     for i in range(n_pool):
         srv.add_scene(S.write_text(S.random_tree(500_000 + i, 2, 2048, 12)))
@@ -690,7 +691,9 @@ def run_serving(args, sub=False, rates=(100, 500, 1000, 2000, 5000), n_req=512):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded scene generator, seeded Poisson arrivals)",
         "config": {"workload": WORKLOADS[5], "config_index": 5, "pool_scenes": n_pool,
-                   "requests_per_rate": n_req, "slots": 4, "max_batch_views": 256,
+                   "requests_per_rate": n_req, "slots": 8, "max_batch_views": 256,
+                   "order": {0: "arrival", 1: "longest first in a batch",
+                             2: "size-aware: earliest deadline first, priority streams"}[args.serve_order],
                    "hbm_budget_bytes": 40 << 30, "setup_s": round(setup_s, 1),
                    "l2": "inputs (1024 resident scenes, ~0.5 GB) and outputs exceed L2 across a run",
                    "parallelism": "single GPU"},
@@ -758,6 +761,9 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-order", type=int, default=2, choices=[0, 1, 2],
+                    help="render server admission order (configuration 5): 0 arrival, 1 longest first in a "
+                         "batch, 2 size-aware (earliest deadline first, priority streams)")
     ap.add_argument("--no-reference-cuda", action="store_true")
     ap.add_argument("--no-roofline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",

@@ -503,9 +503,13 @@ class Server:
     collected with `wait`; `replay` runs an open-loop arrival trace inside the library."""
 
     def __init__(self, hbm_budget=0, slots=0, max_batch_views=0, warp_tile_w=0, planes=0, keep_results=False,
-                 longest_first=False):
+                 longest_first=False, order=None):
+        """order: 0 arrival order, 1 each batch's views longest first, 2 size-aware
+        (earliest deadline first, priority streams); default 1 if longest_first else 0."""
+        if order is None:
+            order = 1 if longest_first else 0
         cfg = csg_server_config(int(hbm_budget), int(slots), int(max_batch_views), int(warp_tile_w), int(planes),
-                                1 if keep_results else 0, 1 if longest_first else 0)
+                                1 if keep_results else 0, int(order))
         h = _vp()
         check(lib().csg_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h

@@ -105,7 +105,8 @@ csgrt::SceneLayout csgrt::scene_layout(size_t n_nodes, size_t n_prims, size_t n_
     l.kids = align16(l.topo + n_nodes * sizeof(int4));
     l.geo = align16(l.kids + n_kids_f4 * sizeof(float4));
     l.color = align16(l.geo + 2 * n_prims * sizeof(float4));
-    l.bvh = align16(l.color + n_prims * sizeof(float4));
+    l.lbox = align16(l.color + n_prims * sizeof(float4));
+    l.bvh = align16(l.lbox + 2 * n_prims * sizeof(float4));
     l.status = align16(l.bvh + n_bvh_f4 * sizeof(float4));
     l.total = align16(l.status + sizeof(unsigned long long));
     return l;
@@ -157,6 +158,8 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
         e = cudaMemcpy(base + off_geo, pk.geo.data(), 2 * np * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
         e = cudaMemcpy(base + off_color, pk.color.data(), np * sizeof(float4), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(base + lay.lbox, pk.lbox.data(), 2 * np * sizeof(float4), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(base + off_status, 0, sizeof(unsigned long long));
     if (e != cudaSuccess) {
         copy_err(err, errlen, std::string("scene upload: ") + cudaGetErrorString(e));
@@ -169,6 +172,7 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.kids = reinterpret_cast<const float4*>(base + off_kids);
     s->dev.geo = reinterpret_cast<const float4*>(base + off_geo);
     s->dev.color = reinterpret_cast<const float4*>(base + off_color);
+    s->dev.lbox = reinterpret_cast<const float4*>(base + lay.lbox);
     s->dev.n_nodes = static_cast<int32_t>(n);
     s->dev.n_prims = static_cast<int32_t>(np);
     s->dev.op_depth = s->tree.op_depth;
@@ -183,6 +187,9 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
     s->dev.rolled = csgrt::use_rolled(s->tree) ? 1 : 0;
     s->dev.short_circuit = csgrt::use_short_circuit(s->tree) ? 1 : 0;
+    s->dev.cylinders = 0;
+    for (const csgrt::RefNode& nd : s->tree.nodes)
+        if (nd.type == csgrt::kCylinder) s->dev.cylinders = 1;
     s->status = reinterpret_cast<unsigned long long*>(base + off_status);
     *out = s;
     return CSG_OK;

@@ -62,6 +62,7 @@ __device__ __forceinline__ BlockSmem block_smem(unsigned char* smem_raw, int liv
 using csgrt::ViewParams;
 
 // Details, shading and the output planes of one finished ray.
+template <bool CYL = true>
 __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long long* status, const dev::Ray& ray,
                                             const dev::Hit& h, bool capped, int x, int y)
 {
@@ -74,7 +75,7 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
     float4 c;
     dev::V3 P = dev::mk(0.f, 0.f, 0.f), N = dev::mk(0.f, 0.f, 0.f);
     if (is_hit) {
-        dev::hit_details(ray, p.scene.geo, h, P, N);
+        dev::hit_details<CYL>(ray, p.scene.geo, h, P, N);
         const float4 col = __ldg(&p.scene.color[h.idx]);
         c = dev::phong(p.cam.v, dev::mk(p.light[0], p.light[1], p.light[2]), P, N, col);
     } else {
@@ -95,7 +96,8 @@ __device__ __forceinline__ void write_pixel(const ViewParams& p, unsigned long l
 // warp-cooperatively); lanes with inside == false only follow the walk.
 // FINE: the scene's fine live mask (single-view renders of large trees) instead of its own.
 // SCU: the unrolled traversal with the operator short-circuit (no effect on rolled ones).
-template <int SD, bool ROLLED, bool FINE = false, bool SCU = false, class Stacks>
+// CYL: the scene may hold cylinders (false: the cylinder code is left out).
+template <int SD, bool ROLLED, bool FINE = false, bool SCU = false, bool CYL = true, class Stacks>
 __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long long* status, uint32_t iter_cap,
                                              int x, int y, bool inside, Stacks& st, const BlockSmem& bs,
                                              const uint16_t* tab, dev::RayFrame frame)
@@ -108,11 +110,11 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     lm.sum = 0;
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h, frame);
     // (the 32-entry class traverses without the mask: dev::kPrune)
-    if constexpr (dev::kPrune<SD>) dev::live_prepass<ROLLED>(ray, inside, p.scene, lm, bs.wstack);
+    if constexpr (dev::kPrune<SD>) dev::live_prepass<ROLLED, CYL>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
     bool capped = false;
-    const dev::Hit h = dev::csg_traverse<SD, ROLLED, SCU>(p.scene, ray, st, tab, lm, iter_cap, &capped);
-    write_pixel(p, status, ray, h, capped, x, y);
+    const dev::Hit h = dev::csg_traverse<SD, ROLLED, SCU, CYL>(p.scene, ray, st, tab, lm, iter_cap, &capped);
+    write_pixel<CYL>(p, status, ray, h, capped, x, y);
 }
 
 __device__ __forceinline__ void load_table(uint16_t* tab)

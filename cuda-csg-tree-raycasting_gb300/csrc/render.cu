@@ -59,10 +59,18 @@ struct RenderParams {
 #define CSG_TILED_CARVEOUT -1
 #endif
 
+// The unrolled variant with the operator short-circuit for scenes that have it (a tuning
+// knob; 0: unrolled scenes traverse without it).
+#ifndef CSG_UNROLLED_SHORT_CIRCUIT
+#define CSG_UNROLLED_SHORT_CIRCUIT 1
+#endif
+
 // FINE: the scene's fine live mask (scenes with scene.fine set; rolled variants only).
 // LOCAL: the per-ray stacks in local memory (rolled scenes with large live masks).
 // SCU: the operator short-circuit in the unrolled variant (scenes with short_circuit set).
-template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU>
+// CYL: the cylinder code (false only for unrolled scenes without cylinders, whose kernel is
+// then smaller: fewer instruction-cache misses).
+template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU, bool CYL>
 __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG_UNROLLED_MIN_BLOCKS)
     render_tiled(const RenderParams p)
 {
@@ -80,11 +88,11 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     const int x = blockIdx.x * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
     const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
-    pix::render_pixel<SD, ROLLED, FINE, SCU>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st,
+    pix::render_pixel<SD, ROLLED, FINE, SCU, CYL>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st,
                                              bs, tab, frame);
 }
 
-template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU = false>
+template <int SD, bool ROLLED, bool FINE, bool LOCAL, bool SCU = false, bool CYL = true>
 cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
 {
     const int words = FINE ? p.view.scene.fine_words : p.view.scene.live_words;
@@ -98,7 +106,7 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
     if (e != cudaSuccess) return e;
     const unsigned long long bit = device < 64 ? 1ull << device : 0ull;
     if (!(attr_set.load(std::memory_order_acquire) & bit) || !bit) {
-        const auto kernel = render_tiled<SD, ROLLED, FINE, LOCAL, SCU>;
+        const auto kernel = render_tiled<SD, ROLLED, FINE, LOCAL, SCU, CYL>;
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)pix::smem_bytes(SD, FINE ? kFineWordsMax : kLiveWordsMax, kThreads, LOCAL));
         if (e == cudaSuccess && CSG_TILED_CARVEOUT >= 0)
@@ -107,7 +115,7 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
         attr_set.fetch_or(bit, std::memory_order_release);
     }
     const dim3 grid((p.view.w + kTileW - 1) / kTileW, (p.view.h + kTileH - 1) / kTileH);
-    render_tiled<SD, ROLLED, FINE, LOCAL, SCU><<<grid, kThreads, smem, stream>>>(p);
+    render_tiled<SD, ROLLED, FINE, LOCAL, SCU, CYL><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
 
@@ -115,13 +123,19 @@ template <int SD>
 cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
 {
     if (!p.view.scene.rolled) {
-        if (SD < 32 && p.view.scene.short_circuit) return launch_variant<SD, false, false, false, true>(p, stream);
-        return launch_variant<SD, false, false, false>(p, stream);
+        const bool sc = CSG_UNROLLED_SHORT_CIRCUIT && SD < 32 && p.view.scene.short_circuit;
+        if (p.view.scene.cylinders)
+            return sc ? launch_variant<SD, false, false, false, true, true>(p, stream)
+                      : launch_variant<SD, false, false, false, false, true>(p, stream);
+        return sc ? launch_variant<SD, false, false, false, true, false>(p, stream)
+                  : launch_variant<SD, false, false, false, false, false>(p, stream);
     }
     if (p.view.scene.fine) return launch_variant<SD, true, true, false>(p, stream);
-    if (CSG_TILED_LOCAL_WORDS >= 0 && p.view.scene.live_words >= CSG_TILED_LOCAL_WORDS)
-        return launch_variant<SD, true, false, true>(p, stream);
-    return launch_variant<SD, true, false, false>(p, stream);
+    const bool local = CSG_TILED_LOCAL_WORDS >= 0 && p.view.scene.live_words >= CSG_TILED_LOCAL_WORDS;
+    if (!p.view.scene.cylinders)
+        return local ? launch_variant<SD, true, false, true, false, false>(p, stream)
+                     : launch_variant<SD, true, false, false, false, false>(p, stream);
+    return local ? launch_variant<SD, true, false, true>(p, stream) : launch_variant<SD, true, false, false>(p, stream);
 }
 
 __global__ void tan_half_fov_kernel(float fov, float* out) { *out = tanf(__fmul_rn(fov, 0.5f)); }

@@ -326,14 +326,19 @@ void use_exact_boxes(HostTree& t)
 #endif
 bool use_prepass(int32_t n_prims) { return n_prims >= CSG_PREPASS_MIN_PRIMS; }
 
-// Build-time tuning knob: trees with cylinders and more primitives than this use the
-// rolled kernel variant.
+// Build-time tuning knobs: trees with cylinders and more primitives than
+// CSG_ROLLED_MIN_PRIMS use the rolled kernel variant; trees without cylinders do too when
+// CSG_ROLLED_WITHOUT_CYLINDERS is 1.
+#ifndef CSG_ROLLED_WITHOUT_CYLINDERS
+#define CSG_ROLLED_WITHOUT_CYLINDERS 1
+#endif
 #ifndef CSG_ROLLED_MIN_PRIMS
 #define CSG_ROLLED_MIN_PRIMS 8
 #endif
 bool use_rolled(const HostTree& tree)
 {
     if (tree.prims.size() <= (size_t)CSG_ROLLED_MIN_PRIMS) return false;
+    if (CSG_ROLLED_WITHOUT_CYLINDERS) return true;
     for (const RefNode& n : tree.nodes)
         if (n.type == kCylinder) return true;
     return false;
@@ -528,6 +533,19 @@ void pack_scene(const HostTree& t, PackedScene& out)
     // batched workload's random trees (oracle, live-leaf pruning and short-circuit on).
     const bool reorder = use_short_circuit(t) && t.op_depth <= 15;
     auto n_leaves = [&](int32_t i) { return t.leaf_hi[i] - t.leaf_lo[i] + 1; };
+    // Depths (operators above a node) and, per leaf, the depth of the deepest operator
+    // above it that does not pass the leaf's record up when the rest of its subtree is a
+    // Miss: an Intersection, or a Difference entered on its right (the single-leaf
+    // shortcut in trace.cuh).  Preorder lists parents before children.
+    std::vector<int32_t> depth(n, 0), blk(n, -1);
+    for (size_t i = 0; i < n; ++i) {
+        const int32_t p = t.nodes[i].parent;
+        if (p < 0) continue;
+        depth[i] = depth[p] + 1;
+        const RefNode& pn = t.nodes[p];
+        const bool passes = pn.type == kUnion || (pn.type == kDifference && pn.left == static_cast<int32_t>(i));
+        blk[i] = passes ? blk[p] : depth[p];
+    }
     out.topo.assign(n, int4{0, 0, 0, 0});
     out.kids.assign(kKidsPerNode * std::max<size_t>(n_ops, 1), float4{0, 0, 0, 0});
     out.geo.assign(2 * np, float4{0, 0, 0, 0});
@@ -556,7 +574,8 @@ void pack_scene(const HostTree& t, PackedScene& out)
         // independent: disjoint leaf ranges, separate hit records).
         auto prio = [](const RefNode& c) { return c.prim == -1 ? 0 : c.type == kSphere ? 1 : c.type == kCube ? 2 : 3; };
         const int32_t swap = prio(r) < prio(l) ? (1 << 30) : 0;
-        k[4] = float4{as_float(t.leaf_lo[li] | swap), as_float(t.leaf_hi[li]), as_float(t.leaf_lo[ri]),
+        const int32_t dc = std::min<int32_t>(depth[i] + 1, 255);
+        k[4] = float4{as_float(t.leaf_lo[li] | swap), as_float(t.leaf_hi[li] | (dc << 16)), as_float(t.leaf_lo[ri]),
                       as_float(t.leaf_hi[ri])};
     }
     // live-mask granularity: one bit per 2^shift leaves, at most kLiveWordsMax words
@@ -585,6 +604,14 @@ void pack_scene(const HostTree& t, PackedScene& out)
         for (size_t i = 0; i < np; ++i) b.idx[i] = static_cast<int32_t>(i);
         out.bvh.resize(4);
         b.build(0, 0, static_cast<int>(np));
+    }
+    out.lbox.assign(2 * np, float4{0, 0, 0, 0});
+    for (size_t i = 0; i < n; ++i) {
+        const RefNode& nd = t.nodes[i];
+        if (nd.prim == -1) continue;
+        const int32_t b = std::min<int32_t>(blk[i] + 1, 255);
+        out.lbox[2 * nd.prim + 0] = float4{nd.minx, nd.miny, nd.minz, as_float(nd.type)};
+        out.lbox[2 * nd.prim + 1] = float4{nd.maxx, nd.maxy, nd.maxz, as_float(nd.prim | (b << 16))};
     }
     for (size_t i = 0; i < np; ++i) {
         const RefPrim& p = t.prims[i];

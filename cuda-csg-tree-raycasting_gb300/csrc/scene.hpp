@@ -60,7 +60,13 @@ void use_exact_boxes(HostTree& t);
 //                     children's leaf ranges:
 //                     {l.min.xyz, l.type} {l.max.xyz, l.prim} {r.min.xyz, r.type}
 //                     {r.max.xyz, r.prim} {l.leaf_lo, l.leaf_hi, r.leaf_lo, r.leaf_hi},
-//                     l.leaf_lo's bit 30 set when the right child is to be tested first
+//                     l.leaf_lo's bit 30 set when the right child is to be tested first,
+//                     the children's depth (operators above them) in bits 16-23 of
+//                     l.leaf_hi
+//   lbox[2p]   per leaf (primitive order) its own box as a kids child record,
+//                     {min.xyz, type} {max.xyz, prim | (blk + 1) << 16}, blk the depth of
+//                     the deepest operator above it that is an Intersection or a Difference
+//                     entered on its right (-1: none), for the single-leaf shortcut
 //   geo[2p]    float4 {cx, cy, cz, p0} {p1, p2, p3, p4}
 //   color[p]   float4 {r, g, b, 0}
 //   bvh[4b]    a binary BVH over the leaves' own boxes (the reference's boxes), used
@@ -102,6 +108,7 @@ struct DeviceScene {
     const float4* kids = nullptr;
     const float4* geo = nullptr;
     const float4* color = nullptr;
+    const float4* lbox = nullptr;
     const float4* bvh = nullptr;
     int32_t n_nodes = 0;
     int32_t n_prims = 0;
@@ -116,6 +123,7 @@ struct DeviceScene {
     int32_t prepass = 0;      // run the liveness pre-pass (scenes with enough leaves)
     int32_t rolled = 0;       // kernel variant: GoTo's tests in a rolled loop (see trace.cuh)
     int32_t short_circuit = 0;  // skip the other child of a Difference / Intersection decided by a Miss
+    int32_t cylinders = 0;      // the tree holds a cylinder
 };
 
 // Host image of the device arrays (for upload and for tests).
@@ -124,6 +132,7 @@ struct PackedScene {
     std::vector<float4> kids;
     std::vector<float4> geo;
     std::vector<float4> color;
+    std::vector<float4> lbox;
     std::vector<float4> bvh;
     int32_t live_words = 0;
     int32_t live_shift = 0;
@@ -144,10 +153,11 @@ int32_t stack_class_for_depth(int32_t op_depth);
 // handful of primitives the pre-pass costs more than the pruning saves).
 bool use_prepass(int32_t n_prims);
 
-// Kernel variant for a tree: the rolled GoTo loop when the tree has cylinders and more
-// than a handful of primitives (the code of three primitive tests unrolled twice overflows
-// the instruction cache), the unrolled one otherwise (it overlaps the two children's
-// tests).
+// Kernel variant for a tree: the rolled GoTo loop when the tree has more than a handful of
+// primitives, the unrolled one (which overlaps the two children's tests) for the smallest.
+// The unrolled code of the primitive tests overflows the instruction cache: 1.7-2.3x slower
+// on trees with cylinders, and since the single-leaf shortcut 14% slower on the cheese
+// frame of spheres (instruction-fetch stalls the top stall reason).
 bool use_rolled(const HostTree& tree);
 
 // Whether the traversal short-circuits Difference and Intersection nodes decided by a Miss

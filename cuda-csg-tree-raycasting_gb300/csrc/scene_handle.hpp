@@ -18,7 +18,7 @@ namespace csgrt {
 
 // Byte offsets of a scene's arrays inside its one device allocation (16-byte aligned).
 struct SceneLayout {
-    size_t topo, kids, geo, color, bvh, status, total;
+    size_t topo, kids, geo, color, lbox, bvh, status, total;
 };
 SceneLayout scene_layout(size_t n_nodes, size_t n_prims, size_t n_kids_f4, size_t n_bvh_f4);
 

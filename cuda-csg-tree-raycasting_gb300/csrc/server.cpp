@@ -60,10 +60,32 @@ constexpr size_t kPlaneAlign = 256;
 // (6% faster than shared-memory stacks on the 1,024-view batch).
 constexpr csgrt::ViewsShape kServerShape{4, true};
 
+// Size-aware scheduling (csg_server_config.order 2).  Requests fall into size levels (up
+// to 2^18 rays, up to 2^20, larger), and a launch holds requests of one level only.  Each
+// request gets a deadline, its arrival plus kDeadlineSlack times its rays at kNominalRate;
+// the dispatcher starts with the earliest deadline whose level may launch and fills the
+// launch with that level's requests, earliest deadlines first.  The two larger levels may
+// have at most kLevelCap launches in flight each, so slots stay free for small requests.
+// A launch runs on a stream whose priority falls with its level, and its blocks take at
+// most kItemsPerWarp warp tiles per warp before they exit, so a launch of small views
+// starts on the SMs as blocks of a running large one retire instead of after all of it.
+constexpr double kNominalRate = 1.5e9;  // rays per second
+constexpr double kDeadlineSlack = 8.0;
+constexpr int kItemsPerWarp = 8;
+constexpr int kPriorityLevels = 3;
+constexpr int kLevelCap[kPriorityLevels] = {kMaxSlots, 2, 2};
+
+int size_level(const csg_request& r)
+{
+    const int64_t rays = (int64_t)r.w * r.h;
+    return rays <= (int64_t(1) << 18) ? 0 : rays <= (int64_t(1) << 20) ? 1 : 2;
+}
+
 struct Req {
     int64_t ticket = 0;
     csg_request r{};
     double t_arrive = 0, t_launch = 0, t_done = 0;
+    double deadline = 0;              // size-aware scheduling: admission order
     int status = CSG_OK;
     int batch_views = 0;
     csgrt::Planes planes{};
@@ -89,6 +111,7 @@ struct PoolScene {
 
 struct Slot {
     cudaStream_t stream = nullptr;
+    cudaStream_t urgent[kPriorityLevels - 1] = {};  // higher-priority streams (size-aware scheduling)
     void* dmem = nullptr;                 // counter, prefix, remaining tiles, view table
     csgrt::ViewRecord* d_views = nullptr;
     int32_t* d_prefix = nullptr;
@@ -110,6 +133,7 @@ struct Launch {
     unsigned int epoch;
     std::vector<Req*> reqs;  // in view-table order
     cudaEvent_t done = nullptr;  // recorded after the launch's last operation
+    int level = -1;          // size level of a size-aware launch
 };
 
 size_t up_align(size_t v)
@@ -182,6 +206,7 @@ struct csg_server {
     int64_t next_ticket = 1, n_done = 0, n_batches = 0, n_evict = 0, n_rejected = 0;
     uint64_t gen = 0;                 // bumped by every event that can unblock admission
     int resident = 0, in_flight = 0;
+    int level_in_flight[kPriorityLevels] = {0, 0, 0};  // size-aware launches in flight per level
     bool stop = false, stop_poll = false;
     std::thread dispatcher, poller;
 
@@ -232,6 +257,7 @@ void csg_server::finish(Launch* L, int status)
             if (q->released) delete q;
         }
         if (L->slot >= 0) slots[L->slot].busy = false;
+        if (L->level >= 0) --level_in_flight[L->level];
         --in_flight;
         ++gen;
     }
@@ -373,6 +399,11 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
         }
         for (size_t i = 0; i < batch.size(); ++i) sc[i] = scenes[batch[i]->r.scene].dev;
     }
+    if (cfg.order == 2 && batch.size() > 1) {
+        // earliest deadline first in the view table too
+        std::stable_sort(batch.begin(), batch.end(), [](const Req* a, const Req* b) { return a->deadline < b->deadline; });
+        for (size_t i = 0; i < batch.size(); ++i) sc[i] = scenes[batch[i]->r.scene].dev;
+    }
     if (cfg.order == 1 && batch.size() > 1) {
         // longest first: the launch's tail is short, at the cost of later completions for
         // the cheap views
@@ -393,7 +424,14 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
         sc.swap(s2);
     }
     cudaStream_t st = alone_form ? alone : slots[slot].stream;
+    int level = -1;
+    if (!alone_form && cfg.order == 2) {
+        level = 0;
+        for (const Req* q : batch) level = std::max(level, size_level(q->r));
+        if (level < kPriorityLevels - 1 && slots[slot].urgent[level]) st = slots[slot].urgent[level];
+    }
     Launch* L = new Launch{this, slot, 0u, batch};
+    L->level = level;
     const int tw = cfg.warp_tile_w;
     cudaError_t e = cudaSuccess;
     if (rc == CSG_OK) {
@@ -453,6 +491,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
                 vl.remaining = S.d_remaining;
                 vl.done_flags = S.d_flags;
                 vl.epoch = L->epoch;
+                vl.items_per_warp = cfg.order == 2 ? kItemsPerWarp : 0;  // (level >= 0)
                 e = csgrt::launch_views(vl, csgrt::stack_class_for_depth(sd), rolled, kServerShape, device, st);
             }
         }
@@ -512,20 +551,47 @@ void csg_server::dispatch_loop()
         });
         if (pending.empty() && stop) break;
 
+        // Size-aware scheduling: the queue in deadline order (stable: equal deadlines keep
+        // their arrival order).
+        if (cfg.order == 2 && pending.size() > 1)
+            std::stable_sort(pending.begin(), pending.end(),
+                             [](const Req* a, const Req* b) { return a->deadline < b->deadline; });
         // Form the next launch: one unbatched request, or a batch for a free slot.
         std::vector<Req*> batch;
         std::vector<csg_scene*> evicted;
         const bool alone_form = (pending.front()->r.flags & CSG_REQ_ALONE) != 0;
         const int slot = alone_form ? -1 : free_slot();
         bool blocked = false, rejected = false;
-        while (!pending.empty() && (int)batch.size() < (alone_form ? 1 : cfg.max_batch_views)) {
-            Req* q = pending.front();
+        // size-aware: the level of the earliest deadline that may launch (-1: none may)
+        int level = -1;
+        if (cfg.order == 2 && !alone_form) {
+            for (const Req* q : pending) {
+                if (q->r.flags & CSG_REQ_ALONE) break;
+                const int l = size_level(q->r);
+                if (level_in_flight[l] < kLevelCap[l]) {
+                    level = l;
+                    break;
+                }
+            }
+            if (level < 0) {
+                // every level with queued requests is at its cap: wait for a launch to end
+                const uint64_t g = gen;
+                cv_work.wait(lk, [&] { return gen != g || stop; });
+                continue;
+            }
+        }
+        for (auto it = pending.begin(); it != pending.end() && (int)batch.size() < (alone_form ? 1 : cfg.max_batch_views);) {
+            Req* q = *it;
             if (((q->r.flags & CSG_REQ_ALONE) != 0) != alone_form) break;
+            if (level >= 0 && size_level(q->r) != level) {
+                ++it;
+                continue;
+            }
             if (!admit(q, evicted)) {
                 blocked = true;
                 break;
             }
-            pending.pop_front();
+            it = pending.erase(it);
             if (q->status != CSG_OK) {
                 complete(q, now());
                 ++n_rejected;
@@ -558,6 +624,7 @@ void csg_server::dispatch_loop()
             continue;
         }
         if (slot >= 0) slots[slot].busy = true;
+        if (level >= 0) ++level_in_flight[level];
         ++in_flight;
         ++n_batches;
         lk.unlock();
@@ -582,7 +649,7 @@ int csg_server_create(const csg_server_config* cfg_in, csg_server** out)
     if (cfg.planes == 0) cfg.planes = CSG_PLANE_RGBA8;
     if (cfg.slots < 1 || cfg.slots > kMaxSlots || cfg.max_batch_views < 1 || cfg.max_batch_views > 4096 ||
         (cfg.warp_tile_w != 4 && cfg.warp_tile_w != 8 && cfg.warp_tile_w != 16 && cfg.warp_tile_w != 32) ||
-        (cfg.planes & ~31) != 0 || cfg.order < 0 || cfg.order > 1)
+        (cfg.planes & ~31) != 0 || cfg.order < 0 || cfg.order > 2)
         return CSG_E_ARG;
     csg_server* s = new (std::nothrow) csg_server();
     if (!s) return CSG_E_CUDA;
@@ -611,6 +678,15 @@ int csg_server_create(const csg_server_config* cfg_in, csg_server** out)
     for (int i = 0; i < cfg.slots && e == cudaSuccess; ++i) {
         Slot& S = s->slots[i];
         e = cudaStreamCreateWithFlags(&S.stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess && cfg.order == 2) {
+            // higher priorities for launches of smaller views (numerically lower is higher)
+            int least = 0, greatest = 0;
+            e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+            for (int k = 0; k < kPriorityLevels - 1 && e == cudaSuccess; ++k) {
+                const int prio = greatest + (least - greatest) * k / (kPriorityLevels - 1);
+                e = cudaStreamCreateWithPriority(&S.urgent[k], cudaStreamNonBlocking, prio);
+            }
+        }
         if (e == cudaSuccess) e = cudaMalloc(&S.dmem, dbytes);
         if (e == cudaSuccess) e = cudaMallocHost(&S.hmem, dbytes);
         if (e == cudaSuccess)
@@ -656,8 +732,11 @@ int csg_server_destroy(csg_server* s)
     }
     s->cv_poll.notify_all();
     if (s->poller.joinable()) s->poller.join();
-    for (int i = 0; i < kMaxSlots; ++i)
+    for (int i = 0; i < kMaxSlots; ++i) {
         if (s->slots[i].stream) cudaStreamSynchronize(s->slots[i].stream);
+        for (cudaStream_t u : s->slots[i].urgent)
+            if (u) cudaStreamSynchronize(u);
+    }
     if (s->alone) cudaStreamSynchronize(s->alone);
     for (auto& kv : s->reqs) {
         if (kv.second->out_mem && !kv.second->free_enqueued) cudaFreeAsync(kv.second->out_mem, s->alone);
@@ -669,6 +748,8 @@ int csg_server_destroy(csg_server* s)
     for (int i = 0; i < kMaxSlots; ++i) {
         Slot& S = s->slots[i];
         if (S.stream) cudaStreamDestroy(S.stream);
+        for (cudaStream_t u : S.urgent)
+            if (u) cudaStreamDestroy(u);
         if (S.dmem) cudaFree(S.dmem);
         if (S.hmem) cudaFreeHost(S.hmem);
         if (S.h_flags) cudaFreeHost(S.h_flags);
@@ -766,6 +847,8 @@ static int submit_at(csg_server* s, const csg_request* r, double t_arrive, int64
         }
         q->ticket = s->next_ticket++;
         q->t_arrive = t_arrive < 0 ? s->now() : t_arrive;
+        // (unbatched requests keep their arrival order: they are the plain form)
+        q->deadline = q->t_arrive + ((r->flags & CSG_REQ_ALONE) ? 0.0 : kDeadlineSlack * (double)r->w * r->h / kNominalRate);
         s->reqs[q->ticket] = q;
         s->pending.push_back(q);
         ++s->gen;

@@ -400,14 +400,16 @@ __device__ __forceinline__ void cube_hit(const Ray& r, float4 g0, int32_t id, Hi
     h.type = kCube;
 }
 
-// hitPrimitive (RaycastingKernels.cu:113-133)
+// hitPrimitive (RaycastingKernels.cu:113-133).  CYL: the scene may hold cylinders (false
+// leaves the cylinder test out of the code: kernels for trees without cylinders).
+template <bool CYL = true>
 __device__ __forceinline__ void hit_primitive(const Ray& r, const float4* __restrict__ geo, int32_t type,
                                               int32_t prim, Hit& h, float tmin)
 {
     const float4 g0 = __ldg(&geo[2 * prim]);
     if (type == kSphere) {
         sphere_hit(r, g0, prim, h, tmin);
-    } else if (type == kCylinder) {
+    } else if (CYL && type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * prim + 1]);
         cylinder_hit(r, g0, g1, prim, h, tmin);
     } else if (type == kCube) {
@@ -669,13 +671,14 @@ constexpr int kWarpStack = 64;
 #ifndef CSG_PREPASS_PRIM_TEST
 #define CSG_PREPASS_PRIM_TEST 1
 #endif
+template <bool CYL>
 __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* __restrict__ geo, int prim,
                                                   int type)
 {
     if (type == kCube || !CSG_PREPASS_PRIM_TEST) return true;
     Hit h = hit_default();
     const float4 g0 = __ldg(&geo[2 * prim]);
-    if (type == kSphere) {
+    if (type == kSphere || !CYL) {
         sphere_hit(ray, g0, prim, h, 0.0f);
     } else {
         const float4 g1 = __ldg(&geo[2 * prim + 1]);
@@ -690,7 +693,7 @@ __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* 
 // (box_may_pass_at_zero) and whose primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
 // active == false only follow.  If the walk would overflow the warp's stack, every lane
 // falls back to an all-live mask (the traversal then decides everything itself).
-template <bool ROLLED, class LM>
+template <bool ROLLED, bool CYL, class LM>
 __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
                                              int* wstack)
 {
@@ -721,13 +724,13 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
                 const int c = j ? cr : cl;
                 const bool h = j ? hr : hl;
                 const int type = __float_as_int(j ? a3.w : a1.w);
-                if (h && c < 0 && leaf_live_at_zero(ray, sc.geo, ~c, type)) lm.set_leaf(~c);
+                if (h && c < 0 && leaf_live_at_zero<CYL>(ray, sc.geo, ~c, type)) lm.set_leaf(~c);
             }
         } else {
             hl = active && box_may_pass_at_zero(ray, a0, a1);
             hr = active && box_may_pass_at_zero(ray, a2, a3);
-            if (hl && cl < 0 && leaf_live_at_zero(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
-            if (hr && cr < 0 && leaf_live_at_zero(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
+            if (hl && cl < 0 && leaf_live_at_zero<CYL>(ray, sc.geo, ~cl, __float_as_int(a1.w))) lm.set_leaf(~cl);
+            if (hr && cr < 0 && leaf_live_at_zero<CYL>(ray, sc.geo, ~cr, __float_as_int(a3.w))) lm.set_leaf(~cr);
         }
         const bool dl = __any_sync(0xffffffffu, hl && cl >= 0);
         const bool dr = __any_sync(0xffffffffu, hr && cr >= 0);
@@ -770,16 +773,70 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 // With boxed == false the same code serves GoTo landing on a leaf (the root is a leaf, or a
 // loop re-enters a leaf child), where the reference calls hitPrimitive with no box test.
 // PRUNE: consult and update the live mask (kPrune<SD>).
-template <bool PRUNE, class LM>
-__device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restrict__ geo, float4 lo, float4 hi,
-                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LM& lm,
-                                           bool boxed = true)
+//
+// Single-leaf shortcut (with PRUNE, one mask bit per leaf, in scenes large enough for the
+// liveness pre-pass: on smaller ones, whose masks start all live, it cost 4%): an operator
+// child of at most
+// kShortcutLeaves leaves with exactly one live leaf l is not descended into.  Every other
+// leaf of it is a Miss at this tmin, and by Kensler's tables a Union with a Miss child
+// returns the other child's record, a Difference returns its left child's record when the
+// right one is a Miss and Miss when the left one is, and an Intersection with a Miss child
+// returns Miss.  So the child's result is l's own (tested with l's box, which every box on
+// the path down to it contains: a box that passes makes every enclosing box pass, a box
+// that culls makes the result a Miss either way) when every operator on that path is a
+// Union or a Difference entered on its left, and a Miss otherwise: l's record in lbox
+// holds the depth of the deepest operator above l that is neither (blk), and the path
+// below a child of depth dc is clear of them when blk < dc.  The descent the reference
+// makes instead pushes and pops in pairs (no stack overflows below the 32-entry class),
+// and it leaves the result in the record of the child's side, as this test does.
+#ifndef CSG_SHORTCUT_LEAVES
+#define CSG_SHORTCUT_LEAVES 128
+#endif
+constexpr int kShortcutLeaves = CSG_SHORTCUT_LEAVES;
+
+// The one live leaf of [lo, hi] (a mask of one bit per leaf), or -1 if there are none or
+// several.
+template <class LM>
+__device__ __forceinline__ int single_live_leaf(LM& lm, int lo, int hi)
 {
+    const int wa = lo >> 5, wb = hi >> 5;
+    int found = -1;
+    for (int k = wa; k <= wb; ++k) {
+        if (!((lm.sum >> k) & 1u)) continue;
+        uint32_t m = lm.word(k);
+        if (k == wa) m &= 0xffffffffu << (lo & 31);
+        if (k == wb) m &= 0xffffffffu >> (31 - (hi & 31));
+        if (!m) continue;
+        if (found >= 0 || (m & (m - 1u))) return -1;
+        found = 32 * k + __ffs(m) - 1;
+    }
+    return found;
+}
+
+template <bool PRUNE, bool CYL, class LM>
+__device__ __forceinline__ bool child_test(const Ray& ray, const DeviceScene& sc, float4 lo, float4 hi,
+                                           int leaf_lo, int leaf_hi, Hit& H, float tmin, LM& lm,
+                                           bool boxed = true, int dc = 0)
+{
+    const float4* __restrict__ geo = sc.geo;
     if (PRUNE && !lm.any(leaf_lo, leaf_hi)) {
         H.hit = kMiss;
         return false;
     }
-    const int32_t prim = __float_as_int(hi.w);
+    int32_t prim = __float_as_int(hi.w);
+    if (PRUNE && kShortcutLeaves > 0 && prim < 0 && sc.prepass && lm.shift == 0 && leaf_hi - leaf_lo < kShortcutLeaves) {
+        const int l = single_live_leaf(lm, leaf_lo, leaf_hi);
+        if (l >= 0) {
+            const float4 b1 = __ldg(&sc.lbox[2 * l + 1]);
+            if ((__float_as_int(b1.w) >> 16) - 1 >= dc) {
+                H.hit = kMiss;  // the path down to l holds an Intersection or a right-entered Difference
+                return false;
+            }
+            lo = __ldg(&sc.lbox[2 * l]);
+            hi = make_float4(b1.x, b1.y, b1.z, __int_as_float(l));
+            prim = l;
+        }
+    }
     if (prim < 0) {
         const bool go = box_hit(ray, lo, hi, tmin);
         if (!go) {
@@ -795,7 +852,7 @@ __device__ __forceinline__ bool child_test(const Ray& ray, const float4* __restr
         if (boxed && H.hit != kMiss && !box_hit(ray, lo, hi, tmin)) H.hit = kMiss;
     } else if (type == kCube) {
         cube_hit(ray, g0, prim, H, tmin);
-    } else if (type == kCylinder) {
+    } else if (CYL && type == kCylinder) {
         if (!boxed || box_hit(ray, lo, hi, tmin)) {
             const float4 g1 = __ldg(&geo[2 * prim + 1]);
             cylinder_hit(ray, g0, g1, prim, H, tmin);
@@ -875,7 +932,7 @@ __device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restr
 {
     const int4 rg = __ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * node + 4]));
     if (right) lm.restore_range(rg.z, rg.w, tmin);
-    else lm.restore_range(rg.x & 0x3fffffff, rg.y, tmin);
+    else lm.restore_range(rg.x & 0x3fffffff, rg.y & 0xffff, tmin);
 }
 
 // Operator short-circuit (a tuning knob; 1 on).  Kensler's tables give Miss for a
@@ -902,8 +959,9 @@ constexpr bool kShortCircuit = CSG_SHORT_CIRCUIT != 0;
 // ROLLED evaluates GoTo's tests (both children of an operator, or the leaf GoTo landed on)
 // in one rolled loop, so the primitive tests exist once in the code; the unrolled form
 // overlaps the two children's tests and is faster when the code stays small (scenes
-// without cylinders).  SCU: the unrolled form with the operator short-circuit.
-template <int SD, bool ROLLED, bool SCU, class Stacks, class LM>
+// without cylinders).  SCU: the unrolled form with the operator short-circuit.  CYL: the scene
+// may hold cylinders.
+template <int SD, bool ROLLED, bool SCU, bool CYL, class Stacks, class LM>
 __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Stacks& st,
                                             const uint16_t* tab, LM& lm)
 {
@@ -943,7 +1001,9 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             int4 rg = make_int4(0, 0, 0, 0);
             if (op) rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
             const int first = (rg.x >> 30) & 1;
+            const int dc = rg.y >> 16;
             rg.x &= 0x3fffffff;
+            rg.y &= 0xffff;
 #pragma unroll 1
             for (int k = 0; k < nj; ++k) {
                 const int j = k ^ first;
@@ -962,7 +1022,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
                 }
                 const bool right = (j == 1) || leaf_right;
                 Hit H = right ? T.R : T.L;
-                const bool go = child_test<kPrune<SD>>(T.ray, geo, lo, hi, rlo, rhi, H, T.tmin, lm, op);
+                const bool go = child_test<kPrune<SD>, CYL>(T.ray, sc, lo, hi, rlo, rhi, H, T.tmin, lm, op, dc);
                 if (right) {
                     T.R = H;
                     gr = go;
@@ -978,11 +1038,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             const float4 k2 = __ldg(&kn[2]);
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
-            gl = child_test<kPrune<SD>>(T.ray, geo, k0, k1, rg.x & 0x3fffffff, rg.y, T.L, T.tmin, lm);
-            gr = child_test<kPrune<SD>>(T.ray, geo, k2, k3, rg.z, rg.w, T.R, T.tmin, lm);
+            const int dc = rg.y >> 16;
+            gl = child_test<kPrune<SD>, CYL>(T.ray, sc, k0, k1, rg.x & 0x3fffffff, rg.y & 0xffff, T.L, T.tmin, lm,
+                                             true, dc);
+            gr = child_test<kPrune<SD>, CYL>(T.ray, sc, k2, k3, rg.z, rg.w, T.R, T.tmin, lm, true, dc);
         } else {
             Hit& H = (T.action & kGotoL) ? T.L : T.R;
-            hit_primitive(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
+            hit_primitive<CYL>(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
             if (kPrune<SD> && H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
         }
         if (op) {
@@ -1066,7 +1128,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
 
 // Whole traversal of one ray.  Returns the final hit (a default Miss if the ray was
 // stopped at iter_cap; *capped is then set).
-template <int SD, bool ROLLED, bool SCU, class Stacks, class LM>
+template <int SD, bool ROLLED, bool SCU, bool CYL, class Stacks, class LM>
 __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ray, Stacks& st,
                                             const uint16_t* tab, LM& lm, uint32_t iter_cap, bool* capped)
 {
@@ -1078,7 +1140,7 @@ __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ra
             *capped = true;
             return hit_default();
         }
-        tracer_step<SD, ROLLED, SCU>(T, sc, st, tab, lm);
+        tracer_step<SD, ROLLED, SCU, CYL>(T, sc, st, tab, lm);
     }
     *capped = false;
     return T.L;
@@ -1086,6 +1148,7 @@ __device__ __forceinline__ Hit csg_traverse(const DeviceScene& sc, const Ray& ra
 
 // Hit details (sphere/cylinder/cubeHitDetails, RaycastingKernels.cu:183-200, 338-373,
 // 436-457): position and the normal, flipped once for Flip and once for Exit.
+template <bool CYL = true>
 __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __restrict__ geo, const Hit& h,
                                             V3& P, V3& N)
 {
@@ -1094,7 +1157,7 @@ __device__ __forceinline__ void hit_details(const Ray& ray, const float4* __rest
     const V3 cen = mk(g0.x, g0.y, g0.z);
     if (h.type == kSphere) {
         N = normalize3(sub3(P, cen));
-    } else if (h.type == kCylinder) {
+    } else if (CYL && h.type == kCylinder) {
         const float4 g1 = __ldg(&geo[2 * h.idx + 1]);
         const V3 V = mk(g1.y, g1.z, g1.w);
         const V3 C = sub_scaled(cen, __fmul_rn(g1.x, 0.5f), V);

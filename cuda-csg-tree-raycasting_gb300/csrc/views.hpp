@@ -39,6 +39,11 @@ struct ViewsLaunch {
     int* remaining;
     unsigned int* done_flags;
     unsigned int epoch;
+    // Work items each warp takes before its block exits (0: persistent, the block runs until
+    // the items are gone).  With a bound the grid holds enough blocks for every item and
+    // blocks retire every few items, so a launch on a higher-priority stream starts as soon
+    // as blocks of this one retire.
+    int32_t items_per_warp = 0;
 };
 
 // Work items of a w x h view: warp tiles of tw x (32 / tw) pixels.

@@ -37,7 +37,7 @@ __global__ void __launch_bounds__(NT, CSG_VIEWS_MIN_BLOCKS * pix::kThreads / NT)
     const int tw = 1 << p.tw_log2, th = 32 >> p.tw_log2;
     const int ox = lane & (tw - 1), oy = lane >> p.tw_log2;
     __syncthreads();  // the table is loaded
-    while (true) {
+    for (int taken = 0; p.items_per_warp == 0 || taken < p.items_per_warp; ++taken) {
         int it = 0, vi = 0;
         if (lane == 0) {
             it = atomicAdd(p.counter, 1);
@@ -115,8 +115,12 @@ cudaError_t launch_views_variant(const ViewsLaunch& l, int device, cudaStream_t 
             }
         }
     }
-    // one block per resident slot, but no more warps than items
-    const int grid = std::max(1, std::min(slots, (l.n_items + NT / 32 - 1) / (NT / 32)));
+    // one block per resident slot, but no more warps than items; with a bound on the items
+    // per warp, enough blocks for every item
+    const int warps_needed = (l.n_items + NT / 32 - 1) / (NT / 32);
+    const int grid = l.items_per_warp > 0
+                         ? std::max(1, (l.n_items + l.items_per_warp * (NT / 32) - 1) / (l.items_per_warp * (NT / 32)))
+                         : std::max(1, std::min(slots, warps_needed));
     if (grid_out) {
         *grid_out = grid;
         return cudaSuccess;

@@ -287,7 +287,11 @@ typedef struct csg_server_config {
     int32_t warp_tile_w;      /* 4, 8, 16 or 32 (0: 8) */
     int32_t planes;           /* CSG_PLANE_* bits rendered per request (0: RGBA8) */
     int32_t keep_results;     /* 1: device planes stay until csg_server_release; 0: freed when done */
-    int32_t order;            /* views of a batch: 0 in arrival order, 1 longest first */
+    int32_t order;            /* 0: requests admitted and laid out in arrival order; 1: the same,
+                                 each batch's views longest first; 2: size-aware, earliest
+                                 deadline first (arrival + 8 x its rays at 1.5 Grays/s), launches
+                                 of smaller views on higher-priority streams, blocks that retire
+                                 every 4 warp tiles */
 } csg_server_config;
 
 #define CSG_REQ_ALONE 1       /* render with its own single-view launch (the unbatched form) */

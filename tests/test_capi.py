@@ -73,7 +73,7 @@ def test_server_rejects_bad_configs_without_gpu(csg):
     lib = csg.lib()
     h = ctypes.c_void_p()
     for bad in (dict(slots=17), dict(slots=-1), dict(max_batch_views=5000), dict(warp_tile_w=6), dict(planes=64),
-                dict(order=2)):
+                dict(order=3), dict(order=-1)):
         cfg = csg.csg_server_config()
         for k, v in bad.items():
             setattr(cfg, k, v)

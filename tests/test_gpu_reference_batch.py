@@ -9,7 +9,8 @@ and a chain deeper than 15 operator levels (the 32-entry class).  Views are a qu
 the workload's size each way, so the reference's planes fit on the host.  They run
 through csg_batch_tune's choice and through forced shapes: 32x1, 16x2 and 4x8 warp tiles,
 2, 4 and 8 warps per block, stacks in shared and in local memory.  The served mix is the serving
-workload's kind: requests of differing scenes and sizes, batched by the render server.
+workload's kind: requests of differing scenes and sizes, batched by the render server with
+the size-aware order the benchmark uses.
 
 Every plane of every view: hit mask and primitive index, t and normal bit for bit, float
 RGBA bit for bit (RGBA8 follows).  The deep chain, whose 32-entry stacks overflow (the
@@ -165,7 +166,7 @@ def test_served_mix_against_reference_kernel(csg):
         w, h = side, int(side * rng.choice([0.5, 0.75, 1.0]))
         reqs.append((sid, csg.Camera.look_at_origin(scenes.seeded_direction(rng), float(rng.uniform(2.5, 4))), w, h))
     light = csg.light_dir()
-    with csg.Server(planes=ALL_PLANES, keep_results=True, slots=3, max_batch_views=8) as srv:
+    with csg.Server(planes=ALL_PLANES, keep_results=True, slots=3, max_batch_views=8, order=2) as srv:
         for t in texts:
             srv.add_scene(t)
         tickets = [srv.submit(csg.Server.request(sid, cam, light, w, h)) for sid, cam, w, h in reqs]

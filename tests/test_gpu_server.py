@@ -63,12 +63,15 @@ def _requests(csg, n, n_scenes, seed, alone_every=0):
 
 
 @pytest.mark.gpu
-def test_server_results_equal_alone_renders(csg):
+@pytest.mark.parametrize("order", [0, 2])
+def test_server_results_equal_alone_renders(csg, order):
+    """order 0: arrival order; 2: size-aware (deadline order, priority streams, blocks that
+    retire every few warp tiles)."""
     import torch
     torch.cuda.set_device(0)
     texts = _scene_texts()
     objs = [csg.Scene(t) for t in texts]
-    with csg.Server(planes=ALL_PLANES, keep_results=True, slots=3, max_batch_views=8) as srv:
+    with csg.Server(planes=ALL_PLANES, keep_results=True, slots=3, max_batch_views=8, order=order) as srv:
         ids = [srv.add_scene(t) for t in texts]
         assert ids == list(range(len(texts)))
         reqs = _requests(csg, 40, len(texts), 5, alone_every=5)

@@ -1,5 +1,5 @@
 """The scene compiler's host-side decisions (csg_tree_plan, no device work): stack class
-from the operator depth, rolled GoTo for trees with cylinders and more than 8 primitives,
+from the operator depth, rolled GoTo for trees of more than 8 primitives,
 live-mask words and granularity, the fine mask of single-view renders (on request) for
 rolled trees of 1,025-2,048 leaves, the operator short-circuit for trees where Differences and
 Intersections are common, and the device layout size."""
@@ -36,7 +36,7 @@ def test_plan_matches_the_rules(csg, seed, leaves):
     assert plan["op_depth"] == _depth(tree)
     d = plan["op_depth"]
     assert plan["stack_class"] == (4 if d <= 4 else 8 if d <= 8 else 12 if d <= 12 else 16 if d <= 15 else 32)
-    assert plan["rolled"] == int(kinds.get("Cylinder", 0) > 0 and n > 8)
+    assert plan["rolled"] == int(n > 8)
     shift = 0
     while (n + (1 << shift) - 1) >> shift > 32 * 32:
         shift += 1
@@ -72,7 +72,7 @@ def test_plan_errors_are_parse_errors(csg):
 def test_plan_of_the_benchmark_scenes(csg):
     from csgrt import scenes
     cheese = csg.plan_tree(scenes.config_scene_text(2, 0))
-    assert cheese["short_circuit"] == 0 and cheese["rolled"] == 0  # one Difference over a Union of spheres
+    assert cheese["short_circuit"] == 0 and cheese["rolled"] == 1  # one Difference over a Union of spheres
     # the README tree: a Difference and an Intersection among four operators (unrolled)
     assert csg.plan_tree(scenes.config_scene_text(1, 0))["short_circuit"] == 1
     assert csg.plan_tree(scenes.config_scene_text(3, 0))["short_circuit"] == 1
