@@ -761,6 +761,8 @@ def main():
     ap.add_argument("--config", type=int, default=2, choices=[1, 2, 3, 4, 5])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--rates", default="100,500,1000,2000,5000",
+                    help="configuration 5: arrival rates of the sweep, req/s, comma-separated")
     ap.add_argument("--serve-order", type=int, default=2, choices=[0, 1, 2],
                     help="render server admission order (configuration 5): 0 arrival, 1 longest first in a "
                          "batch, 2 size-aware (earliest deadline first, priority streams)")
@@ -778,7 +780,7 @@ def main():
     elif args.config == 4:
         run_batch(args)
     elif args.config == 5:
-        run_serving(args)
+        run_serving(args, rates=tuple(int(r) for r in args.rates.split(",")))
     else:
         run_engine(args)
 

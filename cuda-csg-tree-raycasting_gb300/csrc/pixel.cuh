@@ -14,11 +14,11 @@ constexpr int kThreads = 128;  // 4 warps per block: the single-view kernel, the
 // Shared memory of an nt-thread block: the per-ray primitive and time stacks (SD slots;
 // none when the stacks are in local memory), the per-ray live masks (live_words words)
 // with their restore records (one float per region of dev::kLiveRegionWords words) and
-// one BVH stack per warp.
+// one pre-pass scratch area per warp.
 inline size_t smem_bytes(int sd, int live_words, int nt = kThreads, bool local_stacks = false)
 {
     return (local_stacks ? 0 : (size_t)sd * nt * 12) + (size_t)live_words * nt * 4 +
-           (size_t)dev::live_regions(live_words) * nt * 4 + (size_t)(nt / 32) * dev::kWarpStack * 4;
+           (size_t)dev::live_regions(live_words) * nt * 4 + (size_t)(nt / 32) * dev::kWarpScratch * 4;
 }
 
 struct BlockSmem {
@@ -54,7 +54,7 @@ __device__ __forceinline__ BlockSmem block_smem(unsigned char* smem_raw, int liv
     BlockSmem b;
     b.live = reinterpret_cast<uint32_t*>(smem_raw + (LOCAL ? 0 : (size_t)SD * NT * 12));
     b.wstack = reinterpret_cast<int*>(b.live + (size_t)(live_words_alloc + dev::live_regions(live_words_alloc)) * NT) +
-               (threadIdx.x >> 5) * dev::kWarpStack;
+               (threadIdx.x >> 5) * dev::kWarpScratch;
     b.nt = NT;
     return b;
 }

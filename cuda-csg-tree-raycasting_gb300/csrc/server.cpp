@@ -58,22 +58,40 @@ constexpr size_t kPlaneAlign = 256;
 // Block shape of the server's view-table launches: per-ray stacks in local memory, the
 // shape the batch autotuner picks for nearly every tree-size class of the random-tree mix
 // (6% faster than shared-memory stacks on the 1,024-view batch).
-constexpr csgrt::ViewsShape kServerShape{4, true};
+#ifndef CSG_SERVER_LOCAL_STACKS
+#define CSG_SERVER_LOCAL_STACKS 1
+#endif
+constexpr csgrt::ViewsShape kServerShape{CSG_SERVER_LOCAL_STACKS ? 4 : 8, CSG_SERVER_LOCAL_STACKS != 0};
 
 // Size-aware scheduling (csg_server_config.order 2).  Requests fall into size levels (up
 // to 2^18 rays, up to 2^20, larger), and a launch holds requests of one level only.  Each
 // request gets a deadline, its arrival plus kDeadlineSlack times its rays at kNominalRate;
 // the dispatcher starts with the earliest deadline whose level may launch and fills the
-// launch with that level's requests, earliest deadlines first.  The two larger levels may
-// have at most kLevelCap launches in flight each, so slots stay free for small requests.
-// A launch runs on a stream whose priority falls with its level, and its blocks take at
-// most kItemsPerWarp warp tiles per warp before they exit, so a launch of small views
-// starts on the SMs as blocks of a running large one retire instead of after all of it.
+// launch with that level's requests, earliest deadlines first.  The largest level has one
+// launch in flight at a time (its requests run in deadline order, each with the whole GPU)
+// and the middle one two, so slots stay free for small requests.  Launches of the smallest
+// level (kUrgentLevels) run on a raised-priority stream, and no block of any launch runs
+// long: a launch of one view uses the single-view kernel, whose blocks render one pixel
+// tile each, and the view-table kernel's blocks take at most kItemsPerWarp warp tiles per
+// warp before they exit.  So a launch of small views starts on the SMs as blocks of a
+// running large one retire instead of after all of it.
 constexpr double kNominalRate = 1.5e9;  // rays per second
 constexpr double kDeadlineSlack = 8.0;
-constexpr int kItemsPerWarp = 8;
+#ifndef CSG_SERVER_ITEMS_PER_WARP
+#define CSG_SERVER_ITEMS_PER_WARP 8
+#endif
+constexpr int kItemsPerWarp = CSG_SERVER_ITEMS_PER_WARP;
 constexpr int kPriorityLevels = 3;
-constexpr int kLevelCap[kPriorityLevels] = {kMaxSlots, 2, 2};
+#ifndef CSG_SERVER_LARGE_IN_FLIGHT
+#define CSG_SERVER_LARGE_IN_FLIGHT 1
+#endif
+constexpr int kLevelCap[kPriorityLevels] = {kMaxSlots, 2, CSG_SERVER_LARGE_IN_FLIGHT};
+// Levels whose launches run on raised-priority streams (the smallest first).
+#ifndef CSG_SERVER_URGENT_LEVELS
+#define CSG_SERVER_URGENT_LEVELS 1
+#endif
+constexpr int kUrgentLevels = CSG_SERVER_URGENT_LEVELS;
+static_assert(kUrgentLevels >= 0 && kUrgentLevels < kPriorityLevels, "urgent levels");
 
 int size_level(const csg_request& r)
 {
@@ -428,7 +446,7 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
     if (!alone_form && cfg.order == 2) {
         level = 0;
         for (const Req* q : batch) level = std::max(level, size_level(q->r));
-        if (level < kPriorityLevels - 1 && slots[slot].urgent[level]) st = slots[slot].urgent[level];
+        if (level < kUrgentLevels && slots[slot].urgent[level]) st = slots[slot].urgent[level];
     }
     Launch* L = new Launch{this, slot, 0u, batch};
     L->level = level;
@@ -448,7 +466,9 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
         }
     }
     if (rc == CSG_OK && e == cudaSuccess) {
-        if (alone_form) {
+        if (alone_form || (cfg.order == 2 && batch.size() == 1)) {
+            // one view: the single-view kernel (size-aware launches of one request too; its
+            // blocks are short, and the launch's event completes the request)
             Req* q = batch[0];
             csgrt::Camera cam;
             std::memcpy(cam.v, &q->r.cam, sizeof(cam.v));

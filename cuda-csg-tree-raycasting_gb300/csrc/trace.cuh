@@ -662,8 +662,6 @@ struct LiveMaskT {
 using LiveMask = LiveMaskT<live_sum_t>;
 using LiveMaskFine = LiveMaskT<unsigned long long>;
 
-constexpr int kWarpStack = 64;
-
 // Liveness at tmin = 0 of one leaf whose own box already passed at tmin = 0: a cube's box
 // is the cube (the cube test is the same slab test), so it is live; a sphere or cylinder
 // is live when its primitive test at tmin = 0 is not a Miss.
@@ -687,23 +685,23 @@ __device__ __forceinline__ bool leaf_live_at_zero(const Ray& ray, const float4* 
     return h.hit != kMiss;
 }
 
-// Liveness pre-pass: the warp walks the BVH over the leaves' own boxes together (its 32
-// rays are an 8x4 pixel tile, so they share most of the walk), each lane testing its own
-// ray, and every lane sets the bits of the leaves whose box may pass at tmin = 0
-// (box_may_pass_at_zero) and whose primitive test at tmin = 0 is not a Miss.  Must be called by all 32 lanes; lanes with
-// active == false only follow.  If the walk would overflow the warp's stack, every lane
-// falls back to an all-live mask (the traversal then decides everything itself).
+// Per-warp scratch of the liveness pre-pass in shared memory (ints): the stack of the
+// depth-first walk (its first kWarpStack entries) or of the cone walk (all of it).
+constexpr int kWarpStack = 64;
+constexpr int kWarpScratch = 192;
+static_assert(kWarpScratch >= kWarpStack, "warp scratch");
+
+// Liveness pre-pass, depth first: the warp walks the BVH over the leaves' own boxes
+// together (its 32 rays are one pixel tile, so they share most of the walk), each lane
+// testing its own ray, and every lane sets the bits of the leaves whose box may pass at
+// tmin = 0 (box_may_pass_at_zero) and whose primitive test at tmin = 0 is not a Miss.
+// Must be called by all 32 lanes; lanes with active == false only follow.  If the walk
+// would overflow the warp's stack, every lane falls back to an all-live mask (the
+// traversal then decides everything itself).
 template <bool ROLLED, bool CYL, class LM>
-__device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
-                                             int* wstack)
+__device__ __forceinline__ void live_walk_rays(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
+                                               int* wstack, int n_groups)
 {
-    const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
-    lm.reset_records();
-    if (!sc.prepass || sc.n_bvh == 0) {
-        lm.fill(n_groups);
-        return;
-    }
-    lm.clear_all();
     const float4* __restrict__ bvh = sc.bvh;
     int node = 0, sp = 0;
     bool overflow = false;
@@ -754,6 +752,138 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
         __syncwarp();
     }
     if (overflow) lm.fill(n_groups);
+}
+
+// Whether a ray of the cone (apex o, unit axis a, half-angle with sine sp and cosine cp)
+// may meet the box [lo, hi] at t >= 0.  The box is replaced by its bounding sphere, widened
+// by 1e-4 of its radius and of its distance from o, and the test is the signed distance of
+// the sphere's centre from the cone's surface in the plane through the axis: s = d cos -
+// t sin (d the centre's distance from the axis, t its position along it) must not exceed the
+// radius, and u = t cos + d sin must not lie below minus the radius (the sphere is not
+// wholly behind the apex).  Non-finite values pass.
+__device__ __forceinline__ bool cone_may_hit(V3 o, V3 a, float sp, float cp, float4 lo, float4 hi)
+{
+    const float cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
+    const float ex = 0.5f * (hi.x - lo.x), ey = 0.5f * (hi.y - lo.y), ez = 0.5f * (hi.z - lo.z);
+    const float vx = cx - o.x, vy = cy - o.y, vz = cz - o.z;
+    const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
+    const float R = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-4f * dist;
+    const float t = a.x * vx + a.y * vy + a.z * vz;
+    const float qx = a.y * vz - a.z * vy, qy = a.z * vx - a.x * vz, qz = a.x * vy - a.y * vx;
+    const float d = sqrtf(qx * qx + qy * qy + qz * qz);
+    const float s = d * cp - t * sp, u = t * cp + d * sp;
+    return !(s > R) && !(u < -R);
+}
+
+// Liveness pre-pass over a cone: the warp bounds its active lanes' rays by a cone (their
+// mean direction as the axis, the largest angle from it plus 1e-4 rad as the half-angle)
+// and walks the BVH 32 boxes at a time: each step pops up to 32 boxes off a shared stack,
+// one per lane, tests them against the cone (cone_may_hit), pushes the children of the
+// boxes that pass, and has every lane test each leaf that passed with its own ray, as the
+// depth-first walk does (box_may_pass_at_zero and the primitive test at tmin = 0).  So the
+// warp's box tests are shared across the lanes instead of repeated in each.  A box the
+// cone rejects holds no leaf any of the warp's rays can meet: the cone contains every ray,
+// and its margins (1e-4 rad on the angle, 1e-4 relative on the sphere) lie far above the
+// rounding of the rays, of the cone and of the reference's box and primitive tests (~1e-7
+// relative), so no leaf whose tests could pass for some ray is left out.  Returns false,
+// having decided nothing, when the cone is wide (half-angle above 30 degrees, or
+// non-finite) or the stack would overflow; the caller then walks depth first.
+template <bool CYL, class LM>
+__device__ __forceinline__ bool live_walk_cone(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
+                                               int* stk)
+{
+    const unsigned lane = threadIdx.x & 31u;
+    if (!__any_sync(0xffffffffu, active)) return true;  // no lane renders: the masks go unused
+    // cone axis: the mean direction of the active lanes
+    float ax = active ? ray.d.x : 0.f, ay = active ? ray.d.y : 0.f, az = active ? ray.d.z : 0.f;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+        ax += __shfl_xor_sync(0xffffffffu, ax, off);
+        ay += __shfl_xor_sync(0xffffffffu, ay, off);
+        az += __shfl_xor_sync(0xffffffffu, az, off);
+    }
+    const float inv = rsqrtf(ax * ax + ay * ay + az * az);
+    const V3 a = mk(ax * inv, ay * inv, az * inv);
+    // half-angle: the largest sine of the angle between the axis and an active lane's ray
+    float sn = 0.f;
+    bool wide = false;
+    if (active) {
+        const float qx = a.y * ray.d.z - a.z * ray.d.y, qy = a.z * ray.d.x - a.x * ray.d.z,
+                    qz = a.x * ray.d.y - a.y * ray.d.x;
+        sn = sqrtf(qx * qx + qy * qy + qz * qz);
+        wide = !(a.x * ray.d.x + a.y * ray.d.y + a.z * ray.d.z > 0.5f) || !(sn < 0.5f);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) sn = fmaxf(sn, __shfl_xor_sync(0xffffffffu, sn, off));
+    const float sp = sn + 1e-4f;
+    if (__any_sync(0xffffffffu, wide) || !(sp < 0.5f)) return false;
+    const float cp = sqrtf(1.f - sp * sp);
+
+    const float4* __restrict__ bvh = sc.bvh;
+    // stack entries: node << 1 | side (a child slot of a BVH node, whose box is at
+    // bvh[2 * entry] and bvh[2 * entry + 1])
+    if (lane < 2) stk[lane] = (int)lane;  // the root's two children
+    __syncwarp();
+    int n = 2;
+    const unsigned lt = (1u << lane) - 1u;
+    while (n > 0) {
+        const int take = n < 32 ? n : 32;
+        const bool valid = (int)lane < take;
+        const int e = valid ? stk[n - take + (int)lane] : 0;
+        __syncwarp();  // every entry is read before pushes overwrite the slots
+        n -= take;
+        const float4 lo = __ldg(&bvh[2 * e + 0]);
+        const float4 hi = __ldg(&bvh[2 * e + 1]);
+        const bool pass = valid && cone_may_hit(ray.o, a, sp, cp, lo, hi);
+        const int child = __float_as_int(lo.w);
+        const unsigned mi = __ballot_sync(0xffffffffu, pass && child >= 0);
+        unsigned ml = __ballot_sync(0xffffffffu, pass && child < 0);
+        if (n + 2 * __popc(mi) > kWarpScratch) return false;  // warp-uniform
+        if (pass && child >= 0) {
+            const int at = n + 2 * __popc(mi & lt);
+            stk[at] = child << 1;
+            stk[at + 1] = (child << 1) | 1;
+        }
+        n += 2 * __popc(mi);
+        // every lane tests the leaves that passed, each with its own ray
+        while (ml) {
+            const int src = __ffs(ml) - 1;
+            ml &= ml - 1u;
+            const int le = __shfl_sync(0xffffffffu, e, src);
+            const float4 llo = __ldg(&bvh[2 * le + 0]);
+            const float4 lhi = __ldg(&bvh[2 * le + 1]);
+            const int prim = ~__float_as_int(llo.w);
+            if (active && box_may_pass_at_zero(ray, llo, lhi) &&
+                leaf_live_at_zero<CYL>(ray, sc.geo, prim, __float_as_int(lhi.w)))
+                lm.set_leaf(prim);
+        }
+        __syncwarp();
+    }
+    return true;
+}
+
+// Build-time tuning knob: 1 tries the cone walk first, 0 always walks depth first.
+#ifndef CSG_PREPASS_CONE
+#define CSG_PREPASS_CONE 1
+#endif
+
+// Liveness pre-pass: the mask of the leaves each ray can hit at all, at tmin = 0.  Must be
+// called by all 32 lanes; lanes with active == false only follow.
+template <bool ROLLED, bool CYL, class LM>
+__device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const DeviceScene& sc, LM& lm,
+                                             int* wsm)
+{
+    const int n_groups = (sc.n_prims + (1 << lm.shift) - 1) >> lm.shift;
+    lm.reset_records();
+    if (!sc.prepass || sc.n_bvh == 0) {
+        lm.fill(n_groups);
+        return;
+    }
+    lm.clear_all();
+    if (CSG_PREPASS_CONE && live_walk_cone<CYL>(ray, active, sc, lm, wsm)) return;
+    lm.clear_all();
+    __syncwarp();
+    live_walk_rays<ROLLED, CYL>(ray, active, sc, lm, wsm, n_groups);
 }
 
 // One child of an operator node during GoTo (RaycastingKernels.cu:540-553): the box

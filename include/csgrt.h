@@ -288,10 +288,11 @@ typedef struct csg_server_config {
     int32_t planes;           /* CSG_PLANE_* bits rendered per request (0: RGBA8) */
     int32_t keep_results;     /* 1: device planes stay until csg_server_release; 0: freed when done */
     int32_t order;            /* 0: requests admitted and laid out in arrival order; 1: the same,
-                                 each batch's views longest first; 2: size-aware, earliest
-                                 deadline first (arrival + 8 x its rays at 1.5 Grays/s), launches
-                                 of smaller views on higher-priority streams, blocks that retire
-                                 every 4 warp tiles */
+                                 each batch's views longest first; 2: size-aware: requests of
+                                 up to 2^18, up to 2^20 and more rays launched separately,
+                                 earliest deadline first (arrival + 8 x its rays at 1.5 Grays/s),
+                                 one launch of the largest in flight, the smallest on a raised
+                                 stream priority, short-lived blocks */
 } csg_server_config;
 
 #define CSG_REQ_ALONE 1       /* render with its own single-view launch (the unbatched form) */
