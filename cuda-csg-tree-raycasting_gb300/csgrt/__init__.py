@@ -409,6 +409,28 @@ class Scene:
 
 
 # ------------------------------------------------------------------------------------
+def view_array(views):
+    """A csg_view array for (scene, camera, light, w, h, planes) tuples (planes: plane name ->
+    device pointer, as for Batch)."""
+    arr = (csg_view * len(views))()
+    for i, (scene, cam, light, w, h, planes) in enumerate(views):
+        v = arr[i]
+        v.scene = scene.h
+        ctypes.memmove(ctypes.byref(v.cam), ctypes.byref(cam.c), 60)
+        for k in range(3):
+            v.light_dir[k] = float(light[k])
+        v.w, v.h = int(w), int(h)
+        v.out = csg_planes(planes.get("rgba8") or None, planes.get("rgba32f") or None, planes.get("t") or None,
+                           planes.get("prim") or None, planes.get("normal") or None)
+    return arr
+
+
+def render_views_noalloc(views, warp_tile_w=8, stream=None):
+    """csg_render_views_noalloc: the views rendered by one view-table launch whose scratch is
+    the library's fixed device array (asynchronous on `stream`)."""
+    check(lib().csg_render_views_noalloc(view_array(views), len(views), int(warp_tile_w), stream))
+
+
 class Batch:
     """Many views of many scenes rendered by one persistent, graph-replayed launch.
 
@@ -417,16 +439,7 @@ class Batch:
     planes must outlive the batch."""
 
     def __init__(self, views):
-        arr = (csg_view * len(views))()
-        for i, (scene, cam, light, w, h, planes) in enumerate(views):
-            v = arr[i]
-            v.scene = scene.h
-            ctypes.memmove(ctypes.byref(v.cam), ctypes.byref(cam.c), 60)
-            for k in range(3):
-                v.light_dir[k] = float(light[k])
-            v.w, v.h = int(w), int(h)
-            v.out = csg_planes(planes.get("rgba8") or None, planes.get("rgba32f") or None, planes.get("t") or None,
-                               planes.get("prim") or None, planes.get("normal") or None)
+        arr = view_array(views)
         h = _vp()
         check(lib().csg_batch_create(arr, len(views), ctypes.byref(h)))
         self.h = h

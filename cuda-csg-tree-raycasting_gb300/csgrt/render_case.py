@@ -5,6 +5,7 @@ enough to run under a profiler.
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 2 --repeat 2
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 3 --seed 4 --png out.png
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2 --local-stacks
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2 --noalloc
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scene 191 --view-width 1024
 
 Configurations: 1 the README tree at 1280x720, 2 the 512-sphere cheese at 3840x2160,
@@ -37,6 +38,8 @@ def main(argv=None):
     ap.add_argument("--tile", type=int, default=8, help="with --batch-scenes: warp tile width (4, 8, 16, 32)")
     ap.add_argument("--warps", type=int, default=4, help="with --batch-scenes: warps per block (2, 4, 8)")
     ap.add_argument("--local-stacks", action="store_true", help="with --batch-scenes: per-ray stacks in local memory")
+    ap.add_argument("--noalloc", action="store_true",
+                    help="with --batch-scenes: one plain csg_render_views_noalloc launch (no graph) per repeat")
     ap.add_argument("--png", default="", help="write the (single-view) frame as PNG")
     ap.add_argument("--ppm", default="", help="write the (single-view) frame as PPM")
     a = ap.parse_args(argv)
@@ -53,6 +56,12 @@ def main(argv=None):
                 o = torch.empty(v.w * v.h, dtype=torch.int32, device="cuda")
                 outs.append(o)
                 views.append((sc, csgrt.Camera.from_floats(v.camera), v.light, v.w, v.h, {"rgba8": o.data_ptr()}))
+        if a.noalloc:
+            for _ in range(a.repeat):
+                csgrt.render_views_noalloc(views, a.tile)
+            torch.cuda.synchronize()
+            print("noalloc views", len(views))
+            return 0
         b = csgrt.Batch(views)
         b.set_tile(a.tile)
         b.set_shape(a.warps, a.local_stacks)

@@ -291,8 +291,8 @@ typedef struct csg_server_config {
                                  each batch's views longest first; 2: size-aware: requests of
                                  up to 2^18, up to 2^20 and more rays launched separately,
                                  earliest deadline first (arrival + 8 x its rays at 1.5 Grays/s),
-                                 one launch of the largest in flight, the smallest on a raised
-                                 stream priority, short-lived blocks */
+                                 one launch of the largest in flight, each view by the
+                                 single-view kernel, the smallest on a raised stream priority */
 } csg_server_config;
 
 #define CSG_REQ_ALONE 1       /* render with its own single-view launch (the unbatched form) */

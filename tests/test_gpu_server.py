@@ -224,3 +224,41 @@ def test_server_release_while_batch_runs(csg):
         assert st["output_bytes"] == 0
     for o in objs:
         o.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("order", [0, 1, 2])
+def test_server_result_is_complete_when_reported_done(csg, order):
+    """A request counts as done only once its frame is in place: each RGBA8 frame goes to
+    pinned host memory (written by the kernel), pre-filled with a sentinel, and is read on
+    the CPU the moment wait() returns, with no GPU synchronisation in between.  Large views
+    of large trees, alone and batched, in every admission order."""
+    import torch
+    from csgrt import scenes
+    torch.cuda.set_device(0)
+    texts = [scenes.write_text(scenes.random_tree(900 + i, 200, 2048, 12)) for i in range(3)]
+    objs = [csg.Scene(t) for t in texts]
+    rng = np.random.default_rng(31)
+    reqs = []
+    for i in range(18):
+        side = int(rng.choice([64, 512, 1024]))
+        cam = csg.Camera.look_at_origin(scenes.seeded_direction(rng), 3.0)
+        reqs.append((i % 3, cam, csg.light_dir(), side, side, i % 4 == 0))
+    sentinel = np.int32(0x5A5A5A5A)
+    hosts = [torch.full((w * h,), int(sentinel), dtype=torch.int32, pin_memory=True) for *_, w, h, _ in reqs]
+    with csg.Server(slots=3, max_batch_views=4, order=order) as srv:
+        for t in texts:
+            srv.add_scene(t)
+        tickets = [srv.submit(csg.Server.request(sid, cam, light, w, h, alone=a, host_rgba8=hosts[i].data_ptr()))
+                   for i, (sid, cam, light, w, h, a) in enumerate(reqs)]
+        frames = []
+        for t, hb in zip(tickets, hosts):
+            res = srv.wait(t, 120.0)
+            assert res.status == csg.CSG_OK
+            frames.append(hb.numpy().copy())  # at once: no synchronisation with the GPU
+            srv.release(t)
+    for i, (sid, cam, light, w, h, _) in enumerate(reqs):
+        ref = _alone(csg, torch, objs[sid], cam, light, w, h)["rgba8"].cpu().numpy()
+        assert np.array_equal(frames[i], ref), (i, w, int((frames[i] == sentinel).sum()))
+    for o in objs:
+        o.close()
