@@ -68,7 +68,7 @@ int render_common(const csg_scene* s, const csg_camera* cam, const float light[3
     static_assert(sizeof(csg_camera) == sizeof(csgrt::Camera), "camera layout");
     csgrt::Camera c;
     std::memcpy(c.v, cam, sizeof(c.v));
-    const cudaError_t e = csgrt::launch_render(s->dev, c, light, w, h, planes, s->status,
+    const cudaError_t e = csgrt::launch_render(s->dev, s->center, c, light, w, h, planes, s->status,
                                                static_cast<cudaStream_t>(stream));
     return e == cudaSuccess ? CSG_OK : CSG_E_CUDA;
 }
@@ -187,6 +187,12 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.prepass = csgrt::use_prepass(static_cast<int32_t>(np)) ? 1 : 0;
     s->dev.rolled = csgrt::use_rolled(s->tree) ? 1 : 0;
     s->dev.short_circuit = csgrt::use_short_circuit(s->tree) ? 1 : 0;
+    if (!s->tree.nodes.empty()) {
+        const csgrt::RefNode& r = s->tree.nodes[0];
+        s->center[0] = 0.5f * (r.minx + r.maxx);
+        s->center[1] = 0.5f * (r.miny + r.maxy);
+        s->center[2] = 0.5f * (r.minz + r.maxz);
+    }
     s->dev.cylinders = 0;
     for (const csgrt::RefNode& nd : s->tree.nodes)
         if (nd.type == csgrt::kCylinder) s->dev.cylinders = 1;

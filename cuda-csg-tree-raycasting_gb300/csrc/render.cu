@@ -7,7 +7,9 @@
 // a BVH of the leaves), then runs the reference's traversal, skipping subtrees with no
 // live primitive left (trees of up to 15 operator levels; deeper ones, whose stacks can
 // overflow, traverse every subtree as the reference does).
+#include <algorithm>
 #include <atomic>
+#include <cmath>
 
 #include "pixel.cuh"
 
@@ -26,6 +28,8 @@ static_assert(kWarpW == 4 || kWarpW == 8 || kWarpW == 16, "warp tile width");
 
 struct RenderParams {
     pix::ViewParams view;
+    int32_t tiles_x, tiles_y;  // block tiles of the view
+    int32_t center_row;        // block row that starts first (see tile_row)
     unsigned long long* status;
     uint32_t iter_cap;
 };
@@ -65,6 +69,24 @@ struct RenderParams {
 #define CSG_UNROLLED_SHORT_CIRCUIT 1
 #endif
 
+// Block dispatch order (a tuning knob; 0: row by row from the top).  Blocks start in launch
+// order, and the slowest warps of a frame, the ones whose rays cross the most primitives,
+// lie near the object's centre on screen; started late, they ran on alone after the rest
+// of the frame was done (the heaviest batched view's SMs were busy for 40% of its
+// launch).  So block rows go out from the row of the projected centre of the scene's
+// box: row c, then c - 1, c + 1, c - 2, ... (`tile_row`).  Each block's work is unchanged.
+#ifndef CSG_TILED_CENTER_OUT
+#define CSG_TILED_CENTER_OUT 1
+#endif
+
+// The k-th block row to dispatch: c, c - 1, c + 1, c - 2, c + 2, ... within [0, n).
+__device__ __forceinline__ int tile_row(int k, int c, int n)
+{
+    const int m = min(c, n - 1 - c);  // rows on both sides of c
+    if (k <= 2 * m) return (k & 1) ? c - ((k + 1) >> 1) : c + (k >> 1);
+    return (c - m == 0) ? c + m + (k - 2 * m) : c - m - (k - 2 * m);
+}
+
 // FINE: the scene's fine live mask (scenes with scene.fine set; rolled variants only).
 // LOCAL: the per-ray stacks in local memory (rolled scenes with large live masks).
 // SCU: the operator short-circuit in the unrolled variant (scenes with short_circuit set).
@@ -85,8 +107,10 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     const pix::BlockSmem bs =
         pix::block_smem<SD, kThreads, LOCAL>(smem_raw, FINE ? p.view.scene.fine_words : p.view.scene.live_words);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int x = blockIdx.x * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
-    const int y = blockIdx.y * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
+    const int bx = (int)(blockIdx.x % (unsigned)p.tiles_x);
+    const int by = tile_row((int)(blockIdx.x / (unsigned)p.tiles_x), p.center_row, p.tiles_y);
+    const int x = bx * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
+    const int y = by * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
     __syncthreads();
     pix::render_pixel<SD, ROLLED, FINE, SCU, CYL>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st,
                                              bs, tab, frame);
@@ -114,7 +138,7 @@ cudaError_t launch_variant(const RenderParams& p, cudaStream_t stream)
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit, std::memory_order_release);
     }
-    const dim3 grid((p.view.w + kTileW - 1) / kTileW, (p.view.h + kTileH - 1) / kTileH);
+    const unsigned grid = (unsigned)p.tiles_x * (unsigned)p.tiles_y;
     render_tiled<SD, ROLLED, FINE, LOCAL, SCU, CYL><<<grid, kThreads, smem, stream>>>(p);
     return cudaGetLastError();
 }
@@ -161,7 +185,7 @@ cudaError_t device_tan_half_fov(float fov, float* host_out)
     return e;
 }
 
-cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const float light[3],
+cudaError_t launch_render(const DeviceScene& scene, const float center[3], const Camera& cam, const float light[3],
                           int32_t w, int32_t h, const Planes& out,
                           unsigned long long* status, cudaStream_t stream)
 {
@@ -176,6 +200,26 @@ cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const flo
     p.view.out = out;
     p.status = status;
     p.iter_cap = iteration_cap();
+    p.tiles_x = (w + kTileW - 1) / kTileW;
+    p.tiles_y = (h + kTileH - 1) / kTileH;
+    p.center_row = 0;
+    if (CSG_TILED_CENTER_OUT) {
+        // the pixel row of the scene's centre (Raycaster's ray generation inverted:
+        // ny = (1 - 2 v) tan(fov / 2), v = (y + 0.5) / (h - 1)); the middle row if it is not
+        // in front of the camera
+        const float* c = cam.v;
+        const float vx = center[0] - c[0], vy = center[1] - c[1], vz = center[2] - c[2];
+        const float z = vx * c[6] + vy * c[7] + vz * c[8];
+        const float thf = std::tan(0.5f * c[5]);
+        float row = 0.5f * (float)h;
+        if (z > 0.f && thf > 0.f) {
+            const float ny = (vx * c[12] + vy * c[13] + vz * c[14]) / z;
+            row = 0.5f * (1.f - ny / thf) * (float)(h - 1) - 0.5f;
+        }
+        if (!(row >= 0.f)) row = 0.f;  // also NaN
+        if (row > (float)(h - 1)) row = (float)(h - 1);
+        p.center_row = std::min((int)row / kTileH, p.tiles_y - 1);
+    }
     switch (scene.stack_class) {
         case 4: return launch_sd<4>(p, stream);
         case 8: return launch_sd<8>(p, stream);

@@ -39,8 +39,9 @@ uint32_t iteration_cap();
 void set_iteration_cap(uint32_t cap);
 
 // Fused RaycastKernel + LightningKernel for one view of one scene.  `status` is a device
-// counter incremented once per ray that stopped at the iteration cap.
-cudaError_t launch_render(const DeviceScene& scene, const Camera& cam, const float light[3],
+// counter incremented once per ray that stopped at the iteration cap; `center`, the centre
+// of the scene's root box, sets the order in which the pixel tiles start.
+cudaError_t launch_render(const DeviceScene& scene, const float center[3], const Camera& cam, const float light[3],
                           int32_t w, int32_t h, const Planes& out,
                           unsigned long long* status, cudaStream_t stream);
 

@@ -12,6 +12,7 @@ struct csg_scene {
     size_t bytes = 0;
     unsigned long long* status = nullptr;   // rays stopped at the traversal iteration cap
     int device = 0;
+    float center[3] = {0.f, 0.f, 0.f};      // centre of the root's box (block order of single views)
 };
 
 namespace csgrt {

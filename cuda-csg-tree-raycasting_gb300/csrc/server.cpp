@@ -499,7 +499,8 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
                 Req* q = batch[k];
                 csgrt::Camera cam;
                 std::memcpy(cam.v, &q->r.cam, sizeof(cam.v));
-                e = csgrt::launch_render(sc[k]->dev, cam, q->r.light_dir, q->r.w, q->r.h, q->planes, d_capped, st);
+                e = csgrt::launch_render(sc[k]->dev, sc[k]->center, cam, q->r.light_dir, q->r.w, q->r.h, q->planes,
+                                         d_capped, st);
                 if (e == cudaSuccess && !q->copy_back) {
                     {
                         std::lock_guard<std::mutex> g(mu);
@@ -517,7 +518,8 @@ void csg_server::launch(std::vector<Req*>& batch, int slot, bool alone_form)
             Req* q = batch[0];
             csgrt::Camera cam;
             std::memcpy(cam.v, &q->r.cam, sizeof(cam.v));
-            e = csgrt::launch_render(sc[0]->dev, cam, q->r.light_dir, q->r.w, q->r.h, q->planes, d_capped, st);
+            e = csgrt::launch_render(sc[0]->dev, sc[0]->center, cam, q->r.light_dir, q->r.w, q->r.h, q->planes,
+                                     d_capped, st);
         } else {
             // view table in arrival order, tile prefix, per-view remaining tiles
             Slot& S = slots[slot];
