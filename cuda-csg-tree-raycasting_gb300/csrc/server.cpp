@@ -78,7 +78,10 @@ constexpr csgrt::ViewsShape kServerShape{CSG_SERVER_LOCAL_STACKS ? 4 : 8, CSG_SE
 // kItemsPerWarp warp tiles), so a launch of small views starts on the SMs as blocks of a
 // running large one retire instead of after all of it.
 constexpr double kNominalRate = 1.5e9;  // rays per second
-constexpr double kDeadlineSlack = 8.0;
+#ifndef CSG_SERVER_DEADLINE_SLACK
+#define CSG_SERVER_DEADLINE_SLACK 8.0
+#endif
+constexpr double kDeadlineSlack = CSG_SERVER_DEADLINE_SLACK;
 #ifndef CSG_SERVER_ITEMS_PER_WARP
 #define CSG_SERVER_ITEMS_PER_WARP 8
 #endif

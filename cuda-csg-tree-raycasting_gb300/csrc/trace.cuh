@@ -755,19 +755,18 @@ __device__ __forceinline__ void live_walk_rays(const Ray& ray, bool active, cons
 }
 
 // Whether a ray of the cone (apex o, unit axis a, half-angle with sine sp and cosine cp)
-// may meet the box [lo, hi] at t >= 0.  The box is replaced by its bounding sphere, widened
-// by 1e-4 of its radius and of its distance from o, and the test is the signed distance of
-// the sphere's centre from the cone's surface in the plane through the axis: s = d cos -
-// t sin (d the centre's distance from the axis, t its position along it) must not exceed the
-// radius, and u = t cos + d sin must not lie below minus the radius (the sphere is not
-// wholly behind the apex).  Non-finite values pass.
-__device__ __forceinline__ bool cone_may_hit(V3 o, V3 a, float sp, float cp, float4 lo, float4 hi)
+// may meet the sphere of centre c and radius r at t >= 0, the sphere widened by 1e-4 of its
+// radius and by `rel` times its distance from o.  The test is the signed distance of the
+// centre from the cone's surface in the plane through the axis: s = d cos - t sin (d the
+// centre's distance from the axis, t its position along it) must not exceed the radius, and
+// u = t cos + d sin must not lie below minus the radius (the sphere is not wholly behind the
+// apex).  Non-finite values pass.
+__device__ __forceinline__ bool cone_may_hit(V3 o, V3 a, float sp, float cp, float cx, float cy, float cz, float r,
+                                             float rel)
 {
-    const float cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
-    const float ex = 0.5f * (hi.x - lo.x), ey = 0.5f * (hi.y - lo.y), ez = 0.5f * (hi.z - lo.z);
     const float vx = cx - o.x, vy = cy - o.y, vz = cz - o.z;
     const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
-    const float R = sqrtf(ex * ex + ey * ey + ez * ez) * 1.0001f + 1e-4f * dist;
+    const float R = r * 1.0001f + rel * dist;
     const float t = a.x * vx + a.y * vy + a.z * vz;
     const float qx = a.y * vz - a.z * vy, qy = a.z * vx - a.x * vz, qz = a.x * vy - a.y * vx;
     const float d = sqrtf(qx * qx + qy * qy + qz * qz);
@@ -783,9 +782,10 @@ __device__ __forceinline__ bool cone_may_hit(V3 o, V3 a, float sp, float cp, flo
 // depth-first walk does (box_may_pass_at_zero and the primitive test at tmin = 0).  So the
 // warp's box tests are shared across the lanes instead of repeated in each.  A box the
 // cone rejects holds no leaf any of the warp's rays can meet: the cone contains every ray,
-// and its margins (1e-4 rad on the angle, 1e-4 relative on the sphere) lie far above the
-// rounding of the rays, of the cone and of the reference's box and primitive tests (~1e-7
-// relative), so no leaf whose tests could pass for some ray is left out.  Returns false,
+// and its margins (1e-4 rad on the angle, 1e-4 relative on a box's bounding sphere, 1e-3
+// for a sphere leaf tested as itself) lie far above the rounding of the rays, of the cone and
+// of the reference's box and primitive tests (~1e-7 relative), so no leaf whose tests could
+// pass for some ray is left out.  Returns false,
 // having decided nothing, when the cone is wide (half-angle above 30 degrees, or
 // non-finite) or the stack would overflow; the caller then walks depth first.
 template <bool CYL, class LM>
@@ -834,8 +834,21 @@ __device__ __forceinline__ bool live_walk_cone(const Ray& ray, bool active, cons
         n -= take;
         const float4 lo = __ldg(&bvh[2 * e + 0]);
         const float4 hi = __ldg(&bvh[2 * e + 1]);
-        const bool pass = valid && cone_may_hit(ray.o, a, sp, cp, lo, hi);
         const int child = __float_as_int(lo.w);
+        // the bound tested against the cone: a box's bounding sphere, or for a sphere leaf the
+        // sphere itself (its box, +-2r, is 3.5 times wider), widened by 1e-3 of its distance:
+        // a ray that misses the sphere by that much gives a negative discriminant whatever
+        // the rounding (~1e-7 of the squared distance), so the leaf is a Miss at every tmin
+        float cx, cy, cz, r, rel = 1e-4f;
+        if (child < 0 && __float_as_int(hi.w) == kSphere) {
+            const float4 g0 = __ldg(&sc.geo[2 * ~child]);
+            cx = g0.x, cy = g0.y, cz = g0.z, r = fabsf(g0.w), rel = 1e-3f;
+        } else {
+            cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
+            const float ex = 0.5f * (hi.x - lo.x), ey = 0.5f * (hi.y - lo.y), ez = 0.5f * (hi.z - lo.z);
+            r = sqrtf(ex * ex + ey * ey + ez * ez);
+        }
+        const bool pass = valid && cone_may_hit(ray.o, a, sp, cp, cx, cy, cz, r, rel);
         const unsigned mi = __ballot_sync(0xffffffffu, pass && child >= 0);
         unsigned ml = __ballot_sync(0xffffffffu, pass && child < 0);
         if (n + 2 * __popc(mi) > kWarpScratch) return false;  // warp-uniform
