@@ -96,6 +96,29 @@ def cheese_tree(seed: int, n_spheres: int = 512):
 
 
 # ---- configuration 3: random trees ------------------------------------------------------
+def drilled_block(seed: int, n_holes: int = 40):
+    """A cube of edge 2 with n_holes holes cut one after another: a left-deep chain of
+    Differences, Difference(...Difference(Difference(Cube, hole 1), hole 2)..., hole n), so
+    n_holes operator levels (the shape sequential modelling produces).  Holes are
+    axis-aligned cylinders through the block (radius U[0.04, 0.12], height 2.4, centre
+    U[-0.9, 0.9] on the other two axes) and, one in four, spheres (radius U[0.1, 0.3],
+    centre U[-1, 1]^3)."""
+    rng = np.random.default_rng(seed)
+    t = ("Cube", 0.0, 0.0, 0.0, _color(rng), 2.0)
+    rots = ((0.0, 0.0, 0.0), (90.0, 0.0, 0.0), (0.0, 0.0, 90.0))
+    for _ in range(n_holes):
+        col = _color(rng)
+        if rng.random() < 0.25:
+            c = rng.uniform(-1, 1, 3)
+            hole = ("Sphere", c[0], c[1], c[2], col, rng.uniform(0.1, 0.3))
+        else:
+            c = rng.uniform(-0.9, 0.9, 3)
+            rot = rots[int(rng.integers(0, 3))]
+            hole = ("Cylinder", c[0], c[1], c[2], col, rng.uniform(0.04, 0.12), 2.4, *rot)
+        t = ("Difference", t, hole)
+    return t
+
+
 def _random_leaf(rng):
     kind = PRIMITIVES[int(rng.integers(0, 3))]
     c = rng.uniform(-1, 1, 3)

@@ -21,9 +21,10 @@
 //
 // One call renders all its views with one kernel variant: the largest stack class and
 // live mask of its views, and the rolled GoTo loop if any view's scene has it.  The planes
-// are the same whatever the variant, but a single tree deeper than 15 operator levels (the
-// 32-entry stack class, which traverses without live-leaf pruning) makes every view of the
-// call traverse without it, so callers should group views by tree class, as csg_batch does.
+// are the same whatever the variant, but one large tree gives every view of the call its
+// large live mask, and one tree deeper than 15 operator levels its 32-entry stacks (fewer
+// resident blocks, and the guard on every skip), so callers should group views by tree
+// class, as csg_batch does.
 //
 // Only the work counter must start at zero; every call's first fill launch clears it on
 // the call's stream, ahead of the render launch.  Rays stopped at the iteration cap are

@@ -109,8 +109,7 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     lm.words = FINE ? p.scene.fine_words : p.scene.live_words;
     lm.sum = 0;
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h, frame);
-    // (the 32-entry class traverses without the mask: dev::kPrune)
-    if constexpr (dev::kPrune<SD>) dev::live_prepass<ROLLED, CYL>(ray, inside, p.scene, lm, bs.wstack);
+    dev::live_prepass<ROLLED, CYL>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
     bool capped = false;
     const dev::Hit h = dev::csg_traverse<SD, ROLLED, SCU, CYL>(p.scene, ray, st, tab, lm, iter_cap, &capped);

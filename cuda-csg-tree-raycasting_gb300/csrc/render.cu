@@ -5,8 +5,8 @@
 // reference round-trips a 36-byte RayHit per pixel); the only HBM traffic is the output
 // planes.  Each ray first finds the primitives it can hit at all (liveness pre-pass over
 // a BVH of the leaves), then runs the reference's traversal, skipping subtrees with no
-// live primitive left (trees of up to 15 operator levels; deeper ones, whose stacks can
-// overflow, traverse every subtree as the reference does).
+// live primitive left (in trees deeper than 15 operator levels, whose stacks can
+// overflow, only where no push can be dropped: trace.cuh, kGuard).
 #include <algorithm>
 #include <atomic>
 #include <cmath>
@@ -147,7 +147,7 @@ template <int SD>
 cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
 {
     if (!p.view.scene.rolled) {
-        const bool sc = CSG_UNROLLED_SHORT_CIRCUIT && SD < 32 && p.view.scene.short_circuit;
+        const bool sc = CSG_UNROLLED_SHORT_CIRCUIT && p.view.scene.short_circuit;
         if (p.view.scene.cylinders)
             return sc ? launch_variant<SD, false, false, false, true, true>(p, stream)
                       : launch_variant<SD, false, false, false, false, true>(p, stream);

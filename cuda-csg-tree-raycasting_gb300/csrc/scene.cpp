@@ -546,6 +546,14 @@ void pack_scene(const HostTree& t, PackedScene& out)
         const bool passes = pn.type == kUnion || (pn.type == kDifference && pn.left == static_cast<int32_t>(i));
         blk[i] = passes ? blk[p] : depth[p];
     }
+    // Operator heights (0 for a leaf; children follow their parents in preorder).  Trees
+    // deeper than 15 operator levels carry each operator's height, up to 127, in bits 24-30
+    // of the left child's leaf_hi word: the 32-entry stack class skips work under an
+    // operator only where its height leaves the stacks room (trace.cuh, kGuard).
+    std::vector<int32_t> height(n, 0);
+    for (size_t i = n; i-- > 0;)
+        if (t.nodes[i].prim == -1) height[i] = 1 + std::max(height[t.nodes[i].left], height[t.nodes[i].right]);
+    const bool deep = t.op_depth > 15;
     out.topo.assign(n, int4{0, 0, 0, 0});
     out.kids.assign(kKidsPerNode * std::max<size_t>(n_ops, 1), float4{0, 0, 0, 0});
     out.geo.assign(2 * np, float4{0, 0, 0, 0});
@@ -575,8 +583,9 @@ void pack_scene(const HostTree& t, PackedScene& out)
         auto prio = [](const RefNode& c) { return c.prim == -1 ? 0 : c.type == kSphere ? 1 : c.type == kCube ? 2 : 3; };
         const int32_t swap = prio(r) < prio(l) ? (1 << 30) : 0;
         const int32_t dc = std::min<int32_t>(depth[i] + 1, 255);
-        k[4] = float4{as_float(t.leaf_lo[li] | swap), as_float(t.leaf_hi[li] | (dc << 16)), as_float(t.leaf_lo[ri]),
-                      as_float(t.leaf_hi[ri])};
+        const int32_t hb = deep ? std::min<int32_t>(height[i], 127) << 24 : 0;
+        k[4] = float4{as_float(t.leaf_lo[li] | swap), as_float(t.leaf_hi[li] | (dc << 16) | hb),
+                      as_float(t.leaf_lo[ri]), as_float(t.leaf_hi[ri])};
     }
     // live-mask granularity: one bit per 2^shift leaves, at most kLiveWordsMax words
     int32_t shift = 0;

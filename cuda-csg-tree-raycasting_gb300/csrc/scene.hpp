@@ -62,7 +62,8 @@ void use_exact_boxes(HostTree& t);
 //                     {r.max.xyz, r.prim} {l.leaf_lo, l.leaf_hi, r.leaf_lo, r.leaf_hi},
 //                     l.leaf_lo's bit 30 set when the right child is to be tested first,
 //                     the children's depth (operators above them) in bits 16-23 of
-//                     l.leaf_hi
+//                     l.leaf_hi and, in trees deeper than 15 operator levels, the node's
+//                     operator height (up to 127) in bits 24-30 of l.leaf_hi
 //   lbox[2p]   per leaf (primitive order) its own box as a kids child record,
 //                     {min.xyz, type} {max.xyz, prim | (blk + 1) << 16}, blk the depth of
 //                     the deepest operator above it that is an Intersection or a Difference

@@ -915,7 +915,9 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 //
 // With boxed == false the same code serves GoTo landing on a leaf (the root is a leaf, or a
 // loop re-enters a leaf child), where the reference calls hitPrimitive with no box test.
-// PRUNE: consult and update the live mask (kPrune<SD>).
+// PRUNE: consult and update the live mask.  skip_op / skip_leaf: whether a decision that
+// skips work (no live leaf, the single-leaf shortcut) may be taken for an operator child /
+// a leaf (always, except in the 32-entry stack class: kGuard).
 //
 // Single-leaf shortcut (with PRUNE, one mask bit per leaf, in scenes large enough for the
 // liveness pre-pass: on smaller ones, whose masks start all live, it cost 4%): an operator
@@ -930,8 +932,9 @@ __device__ __forceinline__ void live_prepass(const Ray& ray, bool active, const 
 // Union or a Difference entered on its left, and a Miss otherwise: l's record in lbox
 // holds the depth of the deepest operator above l that is neither (blk), and the path
 // below a child of depth dc is clear of them when blk < dc.  The descent the reference
-// makes instead pushes and pops in pairs (no stack overflows below the 32-entry class),
-// and it leaves the result in the record of the child's side, as this test does.
+// makes instead pushes and pops in pairs (none of its pushes is dropped: no stack overflows
+// below the 32-entry class, and in it skip_op holds only where none can, kGuard), and it
+// leaves the result in the record of the child's side, as this test does.
 #ifndef CSG_SHORTCUT_LEAVES
 #define CSG_SHORTCUT_LEAVES 128
 #endif
@@ -959,15 +962,17 @@ __device__ __forceinline__ int single_live_leaf(LM& lm, int lo, int hi)
 template <bool PRUNE, bool CYL, class LM>
 __device__ __forceinline__ bool child_test(const Ray& ray, const DeviceScene& sc, float4 lo, float4 hi,
                                            int leaf_lo, int leaf_hi, Hit& H, float tmin, LM& lm,
-                                           bool boxed = true, int dc = 0)
+                                           bool boxed = true, int dc = 0, bool skip_op = true, bool skip_leaf = true)
 {
     const float4* __restrict__ geo = sc.geo;
-    if (PRUNE && !lm.any(leaf_lo, leaf_hi)) {
+    const bool may_skip = (skip_op && skip_leaf) || (__float_as_int(hi.w) < 0 ? skip_op : skip_leaf);
+    if (PRUNE && may_skip && !lm.any(leaf_lo, leaf_hi)) {
         H.hit = kMiss;
         return false;
     }
     int32_t prim = __float_as_int(hi.w);
-    if (PRUNE && kShortcutLeaves > 0 && prim < 0 && sc.prepass && lm.shift == 0 && leaf_hi - leaf_lo < kShortcutLeaves) {
+    if (PRUNE && skip_op && kShortcutLeaves > 0 && prim < 0 && sc.prepass && lm.shift == 0 &&
+        leaf_hi - leaf_lo < kShortcutLeaves) {
         const int l = single_live_leaf(lm, leaf_lo, leaf_hi);
         if (l >= 0) {
             const float4 b1 = __ldg(&sc.lbox[2 * l + 1]);
@@ -1022,6 +1027,7 @@ struct Tracer {
     int32_t np, ntm;  // primitive / time stack depths (entries in shared memory)
     uint32_t it;
     bool run;
+    bool ok;          // no push of this ray has been dropped (read by the 32-entry class: kGuard)
 
     __device__ __forceinline__ bool busy() const { return run || as.n > 0; }
 };
@@ -1041,6 +1047,7 @@ __device__ __forceinline__ void tracer_begin(Tracer& T, Stacks& st)
     T.as.push(kCompute);
     T.action = kGotoL;
     T.run = true;
+    T.ok = true;
     T.it = 0;
 }
 
@@ -1057,14 +1064,30 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
     }
 }
 
-// Live-leaf pruning per stack class.  Skipping a subtree leaves out pushes and pops that
-// come in pairs only while no stack can overflow: the classes below 32 entries are chosen
-// so that none can, and the 32-entry class, which reproduces the reference's drop-on-full
-// stacks for trees deeper than 15 operator levels, traverses every subtree as the
-// reference does (pruned, the oracle's renders of such trees change wherever a stack
-// overflows).
+// Skipping work per stack class.  Live-leaf pruning, the single-leaf shortcut and the
+// operator short-circuit skip subtrees, and a skipped traversal would have pushed and
+// popped in pairs only if none of its pushes is dropped.  The classes below 32 entries are
+// chosen so that no stack can overflow, and skip freely.  The 32-entry class (kGuard)
+// reproduces the reference's drop-on-full stacks for trees deeper than 15 operator levels,
+// where a push can be dropped; there a skip is taken only while no push of the ray has
+// been dropped (Tracer::ok) and only under an operator whose height h leaves room for the
+// skipped traversal: the operator's own pushes and its child's traversal add at most 2h
+// actions and h entries to each of the other two stacks (two actions and one entry per
+// operator level), so the action depth plus 2h and the other depths plus h must stay
+// within 32 (guard_room).  Before the first dropped push the traversal's state is the one
+// an unbounded stack would hold, where every skip is exact; from the first one on nothing
+// is skipped, and the rest of the traversal is the reference's own.  A leaf's test pushes
+// nothing, so skipping it needs only the first condition.  (Skipping without the guard
+// changes the oracle's renders of such trees wherever a stack overflows.)  The height is
+// in bits 24-30 of the kids record's left leaf_hi, set for trees deeper than 15 levels.
 template <int SD>
-constexpr bool kPrune = SD < 32;
+constexpr bool kGuard = SD >= 32;
+
+template <int SD, class Stacks>
+__device__ __forceinline__ bool guard_room(const Tracer& T, const Stacks& st, int h)
+{
+    return T.ok && T.as.n + 2 * h <= 32 && st.np + h <= SD && st.ntm + h <= SD;
+}
 
 // A loop re-enters one child of operator `node` with a tmin below that of a traversal
 // clear: its leaves in the regions cleared above tmin become live again (the leaf ranges
@@ -1084,9 +1107,9 @@ __device__ __forceinline__ void live_restore_child(LM& lm, const float4* __restr
 // resets both records to the default Miss.  The reference still traverses the other child;
 // skipping it changes no output: the node returns the same default Miss, tmin is restored by
 // SaveLft or set by a loop before any later GoTo reads it, and the stacks are left as the
-// skipped traversal would leave them (it pushes and pops in pairs when no stack can
-// overflow, SD < 32; the 32-entry class reproduces the reference's overflow behaviour, so it
-// always traverses).  Skipped subtrees keep their live bits, which only prunes less.
+// skipped traversal would leave them (it pushes and pops in pairs when none of its pushes
+// is dropped: always below the 32-entry class, and there where guard_room holds).  Skipped
+// subtrees keep their live bits, which only prunes less.
 // Scenes opt in (DeviceScene::short_circuit, chosen by the scene compiler).  The rolled
 // variant carries the code always; the unrolled variant, which serves small trees and
 // sphere/cube scenes such as the cheese frame, carries it only when instantiated with SCU
@@ -1108,24 +1131,43 @@ template <int SD, bool ROLLED, bool SCU, bool CYL, class Stacks, class LM>
 __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, Stacks& st,
                                             const uint16_t* tab, LM& lm)
 {
-    constexpr bool kSC = kShortCircuit && (ROLLED || SCU) && SD < 32;
+    constexpr bool kSC = kShortCircuit && (ROLLED || SCU);
     const int4* __restrict__ topo = sc.topo;
     const float4* __restrict__ kids = sc.kids;
     const float4* __restrict__ geo = sc.geo;
     ++T.it;
     st.np = T.np;
     st.ntm = T.ntm;
+    // The step's pushes.  In the 32-entry class a push onto a full stack (dropped, as the
+    // reference drops it) ends all skipping for the ray (kGuard).
+    auto apush = [&](uint32_t a) {
+        if (kGuard<SD> && T.as.n >= 32) T.ok = false;
+        T.as.push(a);
+    };
+    auto ppush = [&](const Hit& h) {
+        if (kGuard<SD> && st.np >= SD) T.ok = false;
+        st.ppush(h);
+    };
+    auto tpush = [&](float v) {
+        if (kGuard<SD> && st.ntm >= SD) T.ok = false;
+        st.tpush(v);
+    };
+    // the operator height in a kids record's range word (trees deeper than 15 levels)
+    auto height = [](int ry) { return (ry >> 24) & 0x7f; };
     if (T.action & kSaveL) {
         T.tmin = st.tpop();
         if (kSC && sc.short_circuit && (T.L.hit & kMiss) &&
-            (T.ct.w == kDifference || T.ct.w == kIntersection)) {
+            (T.ct.w == kDifference || T.ct.w == kIntersection) &&
+            (!kGuard<SD> ||
+             (T.cur >= 0 &&
+              guard_room<SD>(T, st, height(__ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * T.cur + 4])).y))))) {
             // The left subtree returned a Miss: the node's Compute gives Miss whatever the
             // right subtree returns, so it is not traversed (the pending LoadL is dropped;
             // it would reload this same record).
             T.as.pop();
             T.action = kCompute;
         } else {
-            st.ppush(T.L);
+            ppush(T.L);
             T.action = kGotoR;
         }
     }
@@ -1134,6 +1176,10 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
         T.ct = __ldg(&topo[T.cur]);
         const bool op = T.ct.w <= kIntersection;
         bool gl = false, gr = false;
+        // whether work under this node may be skipped (kGuard): for an operator child and
+        // for a leaf
+        bool skip_op = true;
+        const bool skip_leaf = !kGuard<SD> || T.ok;
         if (ROLLED) {
             // the two children in the order the scene compiler chose (operator children,
             // then spheres, cubes, cylinders), so that a warp's lanes run one kind of test
@@ -1144,7 +1190,8 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             int4 rg = make_int4(0, 0, 0, 0);
             if (op) rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
             const int first = (rg.x >> 30) & 1;
-            const int dc = rg.y >> 16;
+            const int dc = kGuard<SD> ? (rg.y >> 16) & 0xff : rg.y >> 16;
+            if (kGuard<SD>) skip_op = guard_room<SD>(T, st, height(rg.y));
             rg.x &= 0x3fffffff;
             rg.y &= 0xffff;
 #pragma unroll 1
@@ -1165,7 +1212,8 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
                 }
                 const bool right = (j == 1) || leaf_right;
                 Hit H = right ? T.R : T.L;
-                const bool go = child_test<kPrune<SD>, CYL>(T.ray, sc, lo, hi, rlo, rhi, H, T.tmin, lm, op, dc);
+                const bool go =
+                    child_test<true, CYL>(T.ray, sc, lo, hi, rlo, rhi, H, T.tmin, lm, op, dc, skip_op, skip_leaf);
                 if (right) {
                     T.R = H;
                     gr = go;
@@ -1181,14 +1229,15 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             const float4 k2 = __ldg(&kn[2]);
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
-            const int dc = rg.y >> 16;
-            gl = child_test<kPrune<SD>, CYL>(T.ray, sc, k0, k1, rg.x & 0x3fffffff, rg.y & 0xffff, T.L, T.tmin, lm,
-                                             true, dc);
-            gr = child_test<kPrune<SD>, CYL>(T.ray, sc, k2, k3, rg.z, rg.w, T.R, T.tmin, lm, true, dc);
+            const int dc = kGuard<SD> ? (rg.y >> 16) & 0xff : rg.y >> 16;
+            if (kGuard<SD>) skip_op = guard_room<SD>(T, st, height(rg.y));
+            gl = child_test<true, CYL>(T.ray, sc, k0, k1, rg.x & 0x3fffffff, rg.y & 0xffff, T.L, T.tmin, lm, true,
+                                       dc, skip_op, skip_leaf);
+            gr = child_test<true, CYL>(T.ray, sc, k2, k3, rg.z, rg.w, T.R, T.tmin, lm, true, dc, skip_op, skip_leaf);
         } else {
             Hit& H = (T.action & kGotoL) ? T.L : T.R;
             hit_primitive<CYL>(T.ray, geo, T.ct.w, T.ct.x, H, T.tmin);
-            if (kPrune<SD> && H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
+            if (H.hit == kMiss) lm.clear_leaf(T.ct.x, T.tmin);
         }
         if (op) {
             // A child that is not descended into and holds a Miss is a Miss at this tmin
@@ -1196,23 +1245,23 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             // child is such a Miss, or an Intersection with one, computes Miss whatever
             // the other child returns: go straight to Compute.
             const bool lmiss = !gl && (T.L.hit & kMiss), rmiss = !gr && (T.R.hit & kMiss);
-            const bool decided = kSC && sc.short_circuit &&
+            const bool decided = kSC && sc.short_circuit && skip_op &&
                                  ((T.ct.w == kDifference && lmiss) || (T.ct.w == kIntersection && (lmiss || rmiss)));
             if (decided) {
                 T.action = kCompute;
             } else if (gl || gr) {
                 if (!gl) {
-                    st.ppush(T.L);
-                    T.as.push(kLoadL);
+                    ppush(T.L);
+                    apush(kLoadL);
                     T.action = kGotoR;
                 } else if (!gr) {
-                    st.ppush(T.R);
-                    T.as.push(kLoadR);
+                    ppush(T.R);
+                    apush(kLoadR);
                     T.action = kGotoL;
                 } else {
-                    st.tpush(T.tmin);
-                    T.as.push(kLoadL);
-                    T.as.push(kSaveL);
+                    tpush(T.tmin);
+                    apush(kLoadL);
+                    apush(kSaveL);
                     T.action = kGotoL;
                 }
             } else {
@@ -1248,15 +1297,15 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             tracer_parent(T, topo);
         } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
             T.tmin = T.L.t;
-            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false, T.tmin);
-            st.ppush(T.R);
-            T.as.push(kLoadR);
+            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false, T.tmin);
+            ppush(T.R);
+            apush(kLoadR);
             T.action = kGotoL;
         } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
             T.tmin = T.R.t;
-            if (kPrune<SD> && !(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true, T.tmin);
-            st.ppush(T.L);
-            T.as.push(kLoadL);
+            if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true, T.tmin);
+            ppush(T.L);
+            apush(kLoadL);
             T.action = kGotoR;
         } else {
             T.R = hit_default();

@@ -257,8 +257,9 @@ int csg_batch_check(csg_batch* batch, void* stream, uint64_t* n_capped);
  * the one array, so calls whose work may overlap (different streams, unsynchronised
  * threads) race: serialise them.  One call renders all its views with one kernel variant,
  * that of its heaviest view (largest stack class and live mask, rolled if any view is):
- * the planes are the same, but one tree deeper than 15 operator levels turns live-leaf
- * pruning off for every view of the call, so group views by tree class as csg_batch does.
+ * the planes are the same, but one tree deeper than 15 operator levels gives every view of
+ * the call its 32-entry stacks (fewer resident blocks), and one large tree its large live
+ * mask, so group views by tree class as csg_batch does.
  * The call uses about 21 KB of the calling thread's stack. */
 #define CSG_NOALLOC_MAX_VIEWS 4096
 int csg_render_views_noalloc(const csg_view* views, int32_t n_views, int32_t warp_tile_w, void* stream);

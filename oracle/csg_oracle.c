@@ -496,16 +496,24 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * a culled operator child clears the groups inside its leaf range and a leaf that returns
  * Miss its own bit (single-leaf groups only), and each region of orc_live_region groups
  * records the largest tmin at which one of its live groups was cleared; a loop re-enables
- * the looped child's groups in the regions whose record is above its new tmin.  The
- * engine prunes only trees of at most 15 operator levels, whose stacks cannot overflow
- * (deeper trees keep the reference's drop-on-full 32-entry stacks, and skipping a subtree
- * would change which pushes are dropped).  Mode 4 is that rule (the engine's regions are
- * four 32-bit mask words, ORC_LIVE_REGION groups).  Mode 1 is the engine's earlier rule,
+ * the looped child's groups in the regions whose record is above its new tmin.  Mode 4
+ * is the engine's rule (its regions are four 32-bit mask words, ORC_LIVE_REGION groups):
+ * on trees of at most 15 operator levels, whose stacks cannot overflow, as stated here, and
+ * on deeper ones, whose 32-entry stacks can drop pushes, under the guard below.  Mode 1 is the engine's earlier rule,
  * one record per ray raised by every clear, which re-enables whole subtrees that held no
  * stale group; modes 5 and 6 are modes 1 and 4 re-enabling only groups that were live at
  * tmin = 0.  Two unsound variants are kept so that tests can show what the rule's parts
- * prevent: mode 2 leaves out the loop restore, mode 3 prunes trees of any depth.
- * Process-wide. */
+ * prevent: mode 2 leaves out the loop restore, mode 3 prunes trees of any depth without
+ * the guard below.
+ * Trees deeper than 15 operator levels: mode 4 prunes them too, under a guard
+ * (orc_guard_deep, which also covers the operator short-circuit): a skip is taken only
+ * while no push of the ray has been dropped and only where the skipped traversal could
+ * not drop one (under an operator of height h it adds at most 2h actions and h entries to
+ * each of the other stacks, so the action depth plus 2h and the other depths plus h must
+ * stay within 32).  Before the first dropped push the traversal's state is the one an
+ * unbounded stack would hold, where every skip is exact; from the first one on nothing is
+ * skipped, so the rest is the reference's own traversal.  Modes 1, 2, 5 and 6 leave such
+ * trees unpruned.  Process-wide. */
 #define ORC_LIVE_GROUPS 1024
 #define ORC_LIVE_MIN_PRIMS 8
 static int orc_live_mode;
@@ -513,12 +521,39 @@ static int* orc_live_lo;
 static int* orc_live_hi;
 static int orc_live_cap, orc_live_shift, orc_live_nodes, orc_live_prims, orc_live_active;
 void orc_set_live_pruning(int mode) { orc_live_mode = (mode >= 1 && mode <= 6) ? mode : 0; }
+static int* orc_height; /* per node: operator height (0 for a leaf) */
+static int orc_height_cap, orc_guard_deep;
+
+/* Operator heights of every node and the tree's operator depth (operators on the longest
+ * root-to-leaf path); sets orc_guard_deep for trees deeper than 15 levels. */
+static int orc_height_prepare(const orc_node* nodes, int n_nodes)
+{
+    if (n_nodes > orc_height_cap) {
+        int* h = (int*)realloc(orc_height, sizeof(int) * (size_t)n_nodes);
+        if (!h) return -1;
+        orc_height = h;
+        orc_height_cap = n_nodes;
+    }
+    for (int i = n_nodes - 1; i >= 0; --i) {
+        if (nodes[i].prim != -1) {
+            orc_height[i] = 0;
+        } else {
+            const int a = orc_height[nodes[i].left], b = orc_height[nodes[i].right];
+            orc_height[i] = 1 + (a > b ? a : b);
+        }
+    }
+    const int depth = n_nodes > 0 ? orc_height[0] : 0;
+    orc_guard_deep = depth > 15 && orc_live_mode != 3;
+    return depth;
+}
 
 /* Leaf ranges (first and last primitive in preorder) of every node, and the group
  * shift, for the tree about to be rendered. */
 static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
 {
     orc_live_active = 0;
+    const int depth = orc_height_prepare(nodes, n_nodes);
+    if (depth < 0) return -1;
     if (!orc_live_mode) return 0;
     if (n_nodes > orc_live_cap) {
         int* lo = (int*)realloc(orc_live_lo, sizeof(int) * (size_t)n_nodes);
@@ -545,17 +580,7 @@ static int orc_live_prepare(const orc_node* nodes, int n_nodes, int n_prims)
     orc_live_shift = sh;
     orc_live_nodes = n_nodes;
     orc_live_prims = n_prims;
-    /* operator depth: operators on the longest root-to-leaf path (parents precede
-     * their children in preorder) */
-    int depth = 0;
-    int* d = (int*)malloc(sizeof(int) * (size_t)n_nodes);
-    if (!d) return -1;
-    for (int i = 0; i < n_nodes; ++i) {
-        d[i] = (nodes[i].parent >= 0 ? d[nodes[i].parent] : 0) + (nodes[i].prim == -1 ? 1 : 0);
-        if (d[i] > depth) depth = d[i];
-    }
-    free(d);
-    orc_live_active = (orc_live_mode == 3) || depth <= 15;
+    orc_live_active = (orc_live_mode == 3) || (orc_live_mode == 4) || depth <= 15;
     return 0;
 }
 

@@ -5,7 +5,9 @@ bits cleared at the higher tmin changes these rays; the engine marks the looped 
 leaves live again and must match the oracle and the reference kernel bit for bit.  The
 trees and views are ones where the oracle without that restore differs
 (tests/test_live_pruning.py).  Also: trees deeper than 15 operator levels, whose 32-entry
-stacks overflow, where the engine must traverse every subtree as the reference does."""
+stacks can overflow, where the engine skips work only while no push has been dropped and
+where the skipped traversal could not drop one: against the oracle on chains whose stacks
+overflow, and against the reference kernel on drilled blocks whose stacks do not."""
 from __future__ import annotations
 
 import numpy as np
@@ -56,8 +58,10 @@ def test_deep_trees_with_overflowing_stacks_match_oracle(csg, oracle):
     they overflow; the oracle defines those slots as the engine does."""
     from csgrt import scenes
     light = np.float32(csg.light_dir())
-    for seed in DEEP_SEEDS:
-        tree, direction = deep_tree(seed)
+    cases = [deep_tree(seed) for seed in DEEP_SEEDS + (0, 1, 4, 7)]
+    cases += [(scenes.drilled_block(seed, n), scenes.seeded_direction(np.random.default_rng(seed)))
+              for seed, n in ((2, 40), (3, 33))]
+    for seed, (tree, direction) in enumerate(cases):
         text = scenes.write_text(tree)
         with csg.Scene(text) as sc:
             assert sc.info()["stack_class"] == 32
@@ -67,3 +71,30 @@ def test_deep_trees_with_overflowing_stacks_match_oracle(csg, oracle):
         thf = csg.device_tan_half_fov(float(cam[5]))
         ref = oracle.render(nodes, prims, cam, light, 80, 60, mode="fma", tan_half_fov=thf)
         assert_bit_exact(eng, ref, f"deep tree {seed}")
+
+
+@pytest.mark.parametrize("n_holes", [16, 20, 24, 28])
+def test_drilled_blocks_match_reference_kernel(csg, oracle, n_holes):
+    """Drilled blocks of 16-28 holes: deeper than 15 operator levels (the 32-entry class,
+    where skips are guarded), and shallow enough that no stack overflows, so the reference
+    kernel's output is defined: the engine matches it and the oracle bit for bit."""
+    from oracle import RefCuda, quantize_rgba8
+    from csgrt import scenes
+    light = np.float32(csg.light_dir())
+    for seed in range(2):
+        tree = scenes.drilled_block(100 + seed, n_holes)
+        text = scenes.write_text(tree)
+        with csg.Scene(text) as sc:
+            assert sc.info()["stack_class"] == 32
+        cam = csg.Camera.look_at_origin(scenes.seeded_direction(np.random.default_rng(seed)), 3.5).floats()
+        eng = engine_render(csg, text, cam, light, 96, 72)
+        assert int(eng["hit"].sum()) > 1000
+        nodes, prims = oracle.parse(text)
+        thf = csg.device_tan_half_fov(float(cam[5]))
+        ref = oracle.render(nodes, prims, cam, light, 96, 72, mode="fma", tan_half_fov=thf)
+        assert_bit_exact(eng, ref, f"drilled block {n_holes} seed {seed} vs oracle")
+        if RefCuda.available():
+            nodes44, prims48, _ = csg.parse_tree(text)
+            k = RefCuda().render(nodes44, prims48, cam, light, 96, 72)
+            k["rgba8"] = quantize_rgba8(k["rgba"])
+            assert_bit_exact(eng, k, f"drilled block {n_holes} seed {seed} vs reference kernel")

@@ -11,8 +11,10 @@ Without the loop restore the rule is unsound: a node can return its closer child
 a tmin its other child's subtree has already looped to, and an ancestor's loop then re-enters
 that subtree with the lower tmin, where a leaf cleared at the higher tmin can hit.  On trees
 deeper than 15 operator levels, whose 32-entry stacks can overflow, skipping a subtree
-changes which pushes are dropped, so the engine does not prune those.  Two tests render
-trees and views where each part of the rule matters and show the difference."""
+can change which pushes are dropped, so the engine skips there only under a guard: while no
+push of the ray has been dropped, and under an operator whose height leaves the stacks room
+for the skipped traversal.  Tests render trees and views where each part of the rule
+matters and show the difference."""
 from __future__ import annotations
 
 import numpy as np
@@ -105,21 +107,57 @@ def test_live_pruning_reentry_case(csg, oracle):
         assert _differ(ref, _render(oracle, nodes, prims, cam, light, 48, 36, 2, sc)) > 0
 
 
-def test_deep_trees_are_not_pruned(csg, oracle):
-    """The rule leaves trees deeper than 15 operator levels alone; pruning them anyway
-    changes the renders wherever a 32-entry stack overflows."""
+def test_deep_trees_prune_under_the_guard(csg, oracle):
+    """Trees deeper than 15 operator levels: the rule with its guard (mode 4; the
+    short-circuit carries the same guard) keeps every plane of the reference's traversal,
+    with its drop-on-full stacks, on chains whose action stack fills; pruning them without
+    the guard (mode 3) changes the renders wherever a 32-entry stack overflows."""
     from csgrt import scenes
     light = np.float32(csg.light_dir())
-    for seed in DEEP_SEEDS:
+    changed = 0
+    for seed in range(12):
         tree, direction = deep_tree(seed)
         assert scenes.op_depth(tree) > 15
         nodes, prims = oracle.parse(scenes.write_text(tree))
         cam = csg.Camera.look_at_origin(direction, 3.0).floats()
         ref = _render(oracle, nodes, prims, cam, light, 40, 30, 0, False)
-        assert int(ref["counts"]["max_actions"].max()) >= 32  # the action stack fills
-        assert int(ref["hit"].sum()) > 50
-        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 4, False)) == 0
-        assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 3, False)) > 0
+        assert int(ref["counts"]["max_actions"].max()) >= 31  # the action stack (nearly) fills
+        for sc in (False, True):
+            got = _render(oracle, nodes, prims, cam, light, 40, 30, 4, sc)
+            assert _differ(ref, got) == 0, (seed, sc)
+            assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 0, sc)) == 0, (seed, sc)
+        changed += _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 3, False)) > 0
+        if seed in DEEP_SEEDS:
+            assert int(ref["hit"].sum()) > 50
+            assert _differ(ref, _render(oracle, nodes, prims, cam, light, 40, 30, 3, False)) > 0
+    assert changed >= 6
+
+
+def test_drilled_block_prunes_below_the_overflow(csg, oracle):
+    """A cube with holes cut one after another (a left-deep Difference chain): with 20 holes
+    the stacks never fill and the guarded rule skips a third of the iterations (with 24, where
+    only the lowest eight levels leave the stacks room, 14%), every plane unchanged; with 40 the reference's action stack overflows on every ray that enters the
+    chain (the reference then renders the block wrongly: almost no hits), and the guarded rule
+    reproduces that render too."""
+    from csgrt import scenes
+    light = np.float32(csg.light_dir())
+    for seed, n_holes in ((0, 20), (1, 24), (2, 40)):
+        tree = scenes.drilled_block(seed, n_holes)
+        assert scenes.op_depth(tree) == n_holes
+        nodes, prims = oracle.parse(scenes.write_text(tree))
+        rng = np.random.default_rng(seed)
+        cam = csg.Camera.look_at_origin(scenes.seeded_direction(rng), 3.5).floats()
+        ref = _render(oracle, nodes, prims, cam, light, 64, 48, 0, False)
+        got = _render(oracle, nodes, prims, cam, light, 64, 48, 4, True)
+        assert _differ(ref, got) == 0, (seed, n_holes)
+        it0, it4 = int(ref["counts"]["iters"].sum()), int(got["counts"]["iters"].sum())
+        if n_holes <= 24:
+            assert int(ref["counts"]["max_actions"].max()) < 32
+            assert int(ref["hit"].sum()) > 500
+            assert it4 < (0.8 if n_holes == 20 else 0.95) * it0  # less room under 24 levels
+        else:
+            assert int(ref["counts"]["max_actions"].max()) == 32
+            assert int(ref["hit"].sum()) < 50
 
 
 def test_live_pruning_with_non_finite_parameters(csg, oracle):
