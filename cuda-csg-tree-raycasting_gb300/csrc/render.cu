@@ -54,6 +54,11 @@ struct RenderParams {
 #ifndef CSG_TILED_LOCAL_WORDS
 #define CSG_TILED_LOCAL_WORDS 24
 #endif
+// The 32-entry stack class (trees deeper than 15 operator levels) keeps its stacks in local
+// memory (a tuning knob; 0: shared memory, 48 KiB per block, four resident blocks per SM).
+#ifndef CSG_DEEP_LOCAL_STACKS
+#define CSG_DEEP_LOCAL_STACKS 1
+#endif
 // Preferred shared-memory carveout in percent of the maximum (a tuning knob; -1 leaves
 // the choice to the driver, which sizes shared memory for the most resident blocks).
 // Before the operator short-circuit, 80% (five blocks and a larger L1 for the largest live
@@ -155,7 +160,8 @@ cudaError_t launch_sd(const RenderParams& p, cudaStream_t stream)
                   : launch_variant<SD, false, false, false, false, false>(p, stream);
     }
     if (p.view.scene.fine) return launch_variant<SD, true, true, false>(p, stream);
-    const bool local = CSG_TILED_LOCAL_WORDS >= 0 && p.view.scene.live_words >= CSG_TILED_LOCAL_WORDS;
+    const bool local = (CSG_TILED_LOCAL_WORDS >= 0 && p.view.scene.live_words >= CSG_TILED_LOCAL_WORDS) ||
+                       (CSG_DEEP_LOCAL_STACKS && SD >= 32);
     if (!p.view.scene.cylinders)
         return local ? launch_variant<SD, true, false, true, false, false>(p, stream)
                      : launch_variant<SD, true, false, false, false, false>(p, stream);

@@ -1074,20 +1074,23 @@ __device__ __forceinline__ void tracer_parent(Tracer& T, const int4* __restrict_
 // skipped traversal: the operator's own pushes and its child's traversal add at most 2h
 // actions and h entries to each of the other two stacks (two actions and one entry per
 // operator level), so the action depth plus 2h and the other depths plus h must stay
-// within 32 (guard_room).  Before the first dropped push the traversal's state is the one
-// an unbounded stack would hold, where every skip is exact; from the first one on nothing
-// is skipped, and the rest of the traversal is the reference's own.  A leaf's test pushes
-// nothing, so skipping it needs only the first condition.  (Skipping without the guard
-// changes the oracle's renders of such trees wherever a stack overflows.)  The height is
-// in bits 24-30 of the kids record's left leaf_hi, set for trees deeper than 15 levels.
+// within 32.  Every open operator level holds at least as many actions as primitive and
+// time entries together (two actions and a time, or one action and a primitive), and the
+// bottom action is the initial Compute, so while no push has been dropped the primitive and
+// time depths together stay below the action depth where GoTo and SaveLft decide (the
+// oracle checks this on deep chains and random trees): then the action condition implies
+// the other two, and a primitive or time push is never the first to be dropped, so only
+// action pushes are watched (guard_room).  Before the first dropped push the traversal's
+// state is the one an unbounded stack would hold, where every skip is exact; from the first
+// one on nothing is skipped, and the rest of the traversal is the reference's own.  A
+// leaf's test pushes nothing, so skipping it needs only the first condition.  (Skipping
+// without the guard changes the oracle's renders of such trees wherever a stack
+// overflows.)  The height is in bits 24-30 of the kids record's left leaf_hi, set for trees
+// deeper than 15 levels.
 template <int SD>
 constexpr bool kGuard = SD >= 32;
 
-template <int SD, class Stacks>
-__device__ __forceinline__ bool guard_room(const Tracer& T, const Stacks& st, int h)
-{
-    return T.ok && T.as.n + 2 * h <= 32 && st.np + h <= SD && st.ntm + h <= SD;
-}
+__device__ __forceinline__ bool guard_room(const Tracer& T, int h) { return T.ok && T.as.n + 2 * h <= 32; }
 
 // A loop re-enters one child of operator `node` with a tmin below that of a traversal
 // clear: its leaves in the regions cleared above tmin become live again (the leaf ranges
@@ -1138,19 +1141,11 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
     ++T.it;
     st.np = T.np;
     st.ntm = T.ntm;
-    // The step's pushes.  In the 32-entry class a push onto a full stack (dropped, as the
-    // reference drops it) ends all skipping for the ray (kGuard).
+    // The step's action pushes.  In the 32-entry class a push onto a full stack (dropped,
+    // as the reference drops it) ends all skipping for the ray (kGuard).
     auto apush = [&](uint32_t a) {
         if (kGuard<SD> && T.as.n >= 32) T.ok = false;
         T.as.push(a);
-    };
-    auto ppush = [&](const Hit& h) {
-        if (kGuard<SD> && st.np >= SD) T.ok = false;
-        st.ppush(h);
-    };
-    auto tpush = [&](float v) {
-        if (kGuard<SD> && st.ntm >= SD) T.ok = false;
-        st.tpush(v);
     };
     // the operator height in a kids record's range word (trees deeper than 15 levels)
     auto height = [](int ry) { return (ry >> 24) & 0x7f; };
@@ -1160,14 +1155,14 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             (T.ct.w == kDifference || T.ct.w == kIntersection) &&
             (!kGuard<SD> ||
              (T.cur >= 0 &&
-              guard_room<SD>(T, st, height(__ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * T.cur + 4])).y))))) {
+              guard_room(T, height(__ldg(reinterpret_cast<const int4*>(&kids[kKidsPerNode * T.cur + 4])).y))))) {
             // The left subtree returned a Miss: the node's Compute gives Miss whatever the
             // right subtree returns, so it is not traversed (the pending LoadL is dropped;
             // it would reload this same record).
             T.as.pop();
             T.action = kCompute;
         } else {
-            ppush(T.L);
+            st.ppush(T.L);
             T.action = kGotoR;
         }
     }
@@ -1191,7 +1186,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             if (op) rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
             const int first = (rg.x >> 30) & 1;
             const int dc = kGuard<SD> ? (rg.y >> 16) & 0xff : rg.y >> 16;
-            if (kGuard<SD>) skip_op = guard_room<SD>(T, st, height(rg.y));
+            if (kGuard<SD>) skip_op = guard_room(T, height(rg.y));
             rg.x &= 0x3fffffff;
             rg.y &= 0xffff;
 #pragma unroll 1
@@ -1230,7 +1225,7 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
             const float4 k3 = __ldg(&kn[3]);
             const int4 rg = __ldg(reinterpret_cast<const int4*>(&kn[4]));
             const int dc = kGuard<SD> ? (rg.y >> 16) & 0xff : rg.y >> 16;
-            if (kGuard<SD>) skip_op = guard_room<SD>(T, st, height(rg.y));
+            if (kGuard<SD>) skip_op = guard_room(T, height(rg.y));
             gl = child_test<true, CYL>(T.ray, sc, k0, k1, rg.x & 0x3fffffff, rg.y & 0xffff, T.L, T.tmin, lm, true,
                                        dc, skip_op, skip_leaf);
             gr = child_test<true, CYL>(T.ray, sc, k2, k3, rg.z, rg.w, T.R, T.tmin, lm, true, dc, skip_op, skip_leaf);
@@ -1251,15 +1246,15 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
                 T.action = kCompute;
             } else if (gl || gr) {
                 if (!gl) {
-                    ppush(T.L);
+                    st.ppush(T.L);
                     apush(kLoadL);
                     T.action = kGotoR;
                 } else if (!gr) {
-                    ppush(T.R);
+                    st.ppush(T.R);
                     apush(kLoadR);
                     T.action = kGotoL;
                 } else {
-                    tpush(T.tmin);
+                    st.tpush(T.tmin);
                     apush(kLoadL);
                     apush(kSaveL);
                     T.action = kGotoL;
@@ -1298,13 +1293,13 @@ __device__ __forceinline__ void tracer_step(Tracer& T, const DeviceScene& sc, St
         } else if ((acts & hLoopL) || ((acts & hLoopLC) && lt)) {
             T.tmin = T.L.t;
             if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, false, T.tmin);
-            ppush(T.R);
+            st.ppush(T.R);
             apush(kLoadR);
             T.action = kGotoL;
         } else if ((acts & hLoopR) || ((acts & hLoopRC) && gt)) {
             T.tmin = T.R.t;
             if (!(T.tmin >= lm.tclr) && T.cur >= 0) live_restore_child(lm, kids, T.cur, true, T.tmin);
-            ppush(T.L);
+            st.ppush(T.L);
             apush(kLoadL);
             T.action = kGotoR;
         } else {
