@@ -178,7 +178,7 @@ int csg_scene_create_ex(const char* text, size_t len, int32_t flags, csg_scene**
     s->dev.op_depth = s->tree.op_depth;
     s->dev.stack_class = csgrt::stack_class_for_depth(s->tree.op_depth);
     s->dev.bvh = reinterpret_cast<const float4*>(base + off_bvh);
-    s->dev.n_bvh = static_cast<int32_t>(pk.bvh.size() / 4);
+    s->dev.n_bvh = pk.bvh_nodes;
     s->dev.live_words = pk.live_words;
     s->dev.live_shift = pk.live_shift;
     s->dev.fine = (pk.fine || ((flags & CSG_SCENE_FINE_MASK) && csgrt::fine_mask_possible(s->tree, pk))) ? 1 : 0;

@@ -613,6 +613,33 @@ void pack_scene(const HostTree& t, PackedScene& out)
         for (size_t i = 0; i < np; ++i) b.idx[i] = static_cast<int32_t>(i);
         out.bvh.resize(4);
         b.build(0, 0, static_cast<int>(np));
+        // bounding spheres of the slots, for the pre-pass's warp-wide cone test
+        const size_t nb = out.bvh.size() / 4;
+        out.bvh_nodes = static_cast<int32_t>(nb);
+        for (size_t e = 0; e < 2 * nb; ++e) {
+            const float4 lo = out.bvh[2 * e], hi = out.bvh[2 * e + 1];
+            int32_t child, ty;
+            std::memcpy(&child, &lo.w, 4);
+            std::memcpy(&ty, &hi.w, 4);
+            if (child < 0 && ty == kSphere) {
+                const RefPrim& p = t.prims[static_cast<size_t>(~child)];
+                out.bvh.push_back(float4{p.x, p.y, p.z, -std::fabs(p.p[0])});
+                continue;
+            }
+            const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+            float c[3];
+            double r2 = 0.0;
+            for (int k = 0; k < 3; ++k) {
+                c[k] = static_cast<float>(0.5 * (static_cast<double>(l[k]) + static_cast<double>(h[k])));
+                const double d = std::max(std::fabs(static_cast<double>(l[k]) - c[k]), std::fabs(static_cast<double>(h[k]) - c[k]));
+                r2 += d * d;
+            }
+            float r = static_cast<float>(std::sqrt(r2));
+            if (static_cast<double>(r) < std::sqrt(r2)) r = std::nextafter(r, INFINITY);
+            if (!std::isfinite(r) || !std::isfinite(c[0]) || !std::isfinite(c[1]) || !std::isfinite(c[2]))
+                r = INFINITY;  // (a non-finite box always passes)
+            out.bvh.push_back(float4{c[0], c[1], c[2], r});
+        }
     }
     out.lbox.assign(2 * np, float4{0, 0, 0, 0});
     for (size_t i = 0; i < n; ++i) {

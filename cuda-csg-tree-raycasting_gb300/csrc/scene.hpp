@@ -70,10 +70,14 @@ void use_exact_boxes(HostTree& t);
 //                     entered on its right (-1: none), for the single-leaf shortcut
 //   geo[2p]    float4 {cx, cy, cz, p0} {p1, p2, p3, p4}
 //   color[p]   float4 {r, g, b, 0}
-//   bvh[4b]    a binary BVH over the leaves' own boxes (the reference's boxes), used
+//   bvh[6b]    a binary BVH over the leaves' own boxes (the reference's boxes), used
 //                     only to find the primitives a ray can hit; per node the two
 //                     children's boxes: {min.xyz, child} {max.xyz, type} x 2, where
-//                     child >= 0 is a BVH node and child < 0 is leaf ~prim (type valid)
+//                     child >= 0 is a BVH node and child < 0 is leaf ~prim (type valid);
+//                     then per slot (node * 2 + side) a bounding sphere {centre.xyz, r}:
+//                     the smallest ball about the box's rounded centre that holds the box,
+//                     its radius rounded up, or for a sphere leaf the sphere itself with
+//                     its radius negated (the sign marks a sphere leaf)
 // ---------------------------------------------------------------------------------
 constexpr int kKidsPerNode = 5;
 // Node numbering of the device arrays (a build-time knob): 1 numbers the operators first
@@ -134,7 +138,8 @@ struct PackedScene {
     std::vector<float4> geo;
     std::vector<float4> color;
     std::vector<float4> lbox;
-    std::vector<float4> bvh;
+    std::vector<float4> bvh;  // 4 * bvh_nodes slot records, then 2 * bvh_nodes bounding spheres
+    int32_t bvh_nodes = 0;
     int32_t live_words = 0;
     int32_t live_shift = 0;
     int32_t fine = 0;

@@ -760,16 +760,20 @@ __device__ __forceinline__ void live_walk_rays(const Ray& ray, bool active, cons
 // centre from the cone's surface in the plane through the axis: s = d cos - t sin (d the
 // centre's distance from the axis, t its position along it) must not exceed the radius, and
 // u = t cos + d sin must not lie below minus the radius (the sphere is not wholly behind the
-// apex).  Non-finite values pass.
+// apex).  The two distances come from the hardware's reciprocal square root (within a few
+// units of 2^-23 relative, far inside the 1e-4 margins).  Non-finite values pass (a zero
+// distance gives 0 * inf = NaN, which passes too).
 __device__ __forceinline__ bool cone_may_hit(V3 o, V3 a, float sp, float cp, float cx, float cy, float cz, float r,
                                              float rel)
 {
     const float vx = cx - o.x, vy = cy - o.y, vz = cz - o.z;
-    const float dist = sqrtf(vx * vx + vy * vy + vz * vz);
+    const float dd = vx * vx + vy * vy + vz * vz;
+    const float dist = dd * rsqrtf(dd);
     const float R = r * 1.0001f + rel * dist;
     const float t = a.x * vx + a.y * vy + a.z * vz;
     const float qx = a.y * vz - a.z * vy, qy = a.z * vx - a.x * vz, qz = a.x * vy - a.y * vx;
-    const float d = sqrtf(qx * qx + qy * qy + qz * qz);
+    const float q2 = qx * qx + qy * qy + qz * qz;
+    const float d = q2 * rsqrtf(q2);
     const float s = d * cp - t * sp, u = t * cp + d * sp;
     return !(s > R) && !(u < -R);
 }
@@ -820,8 +824,9 @@ __device__ __forceinline__ bool live_walk_cone(const Ray& ray, bool active, cons
     const float cp = sqrtf(1.f - sp * sp);
 
     const float4* __restrict__ bvh = sc.bvh;
+    const float4* __restrict__ bsph = sc.bvh + 4 * sc.n_bvh;
     // stack entries: node << 1 | side (a child slot of a BVH node, whose box is at
-    // bvh[2 * entry] and bvh[2 * entry + 1])
+    // bvh[2 * entry] and bvh[2 * entry + 1] and whose bounding sphere is at bsph[entry])
     if (lane < 2) stk[lane] = (int)lane;  // the root's two children
     __syncwarp();
     int n = 2;
@@ -832,23 +837,15 @@ __device__ __forceinline__ bool live_walk_cone(const Ray& ray, bool active, cons
         const int e = valid ? stk[n - take + (int)lane] : 0;
         __syncwarp();  // every entry is read before pushes overwrite the slots
         n -= take;
-        const float4 lo = __ldg(&bvh[2 * e + 0]);
-        const float4 hi = __ldg(&bvh[2 * e + 1]);
-        const int child = __float_as_int(lo.w);
-        // the bound tested against the cone: a box's bounding sphere, or for a sphere leaf the
-        // sphere itself (its box, +-2r, is 3.5 times wider), widened by 1e-3 of its distance:
-        // a ray that misses the sphere by that much gives a negative discriminant whatever
-        // the rounding (~1e-7 of the squared distance), so the leaf is a Miss at every tmin
-        float cx, cy, cz, r, rel = 1e-4f;
-        if (child < 0 && __float_as_int(hi.w) == kSphere) {
-            const float4 g0 = __ldg(&sc.geo[2 * ~child]);
-            cx = g0.x, cy = g0.y, cz = g0.z, r = fabsf(g0.w), rel = 1e-3f;
-        } else {
-            cx = 0.5f * (lo.x + hi.x), cy = 0.5f * (lo.y + hi.y), cz = 0.5f * (lo.z + hi.z);
-            const float ex = 0.5f * (hi.x - lo.x), ey = 0.5f * (hi.y - lo.y), ez = 0.5f * (hi.z - lo.z);
-            r = sqrtf(ex * ex + ey * ey + ez * ez);
-        }
-        const bool pass = valid && cone_may_hit(ray.o, a, sp, cp, cx, cy, cz, r, rel);
+        const int child = __float_as_int(__ldg(&bvh[2 * e + 0]).w);
+        // the bound tested against the cone (precomputed per slot): a box's bounding sphere,
+        // or for a sphere leaf (negative radius) the sphere itself (its box, +-2r, is 3.5 times
+        // wider), widened by 1e-3 of its distance: a ray that misses the sphere by that much
+        // gives a negative discriminant whatever the rounding (~1e-7 of the squared
+        // distance), so the leaf is a Miss at every tmin
+        const float4 bs = __ldg(&bsph[e]);
+        const float rel = __float_as_int(bs.w) < 0 ? 1e-3f : 1e-4f;
+        const bool pass = valid && cone_may_hit(ray.o, a, sp, cp, bs.x, bs.y, bs.z, fabsf(bs.w), rel);
         const unsigned mi = __ballot_sync(0xffffffffu, pass && child >= 0);
         unsigned ml = __ballot_sync(0xffffffffu, pass && child < 0);
         if (n + 2 * __popc(mi) > kWarpScratch) return false;  // warp-uniform
