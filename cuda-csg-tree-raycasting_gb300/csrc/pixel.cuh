@@ -111,6 +111,14 @@ __device__ __forceinline__ void render_pixel(const ViewParams& p, unsigned long 
     const dev::Ray ray = dev::primary_ray(p.cam.v, inside ? x : 0, inside ? y : 0, (float)p.w, (float)p.h, frame);
     dev::live_prepass<ROLLED, CYL>(ray, inside, p.scene, lm, bs.wstack);
     if (!inside) return;
+    // No live leaf: every leaf is a Miss at every tmin >= 0 (the pre-pass clears a bit only
+    // for such a leaf), so every record the traversal could make or reload is a Miss, no table
+    // cell loops on two Misses, and the ray ends as a Miss: the background, without a
+    // traversal (in the 32-entry class too: whatever its stacks drop, they hold only Misses).
+    if (lm.sum == 0) {
+        write_pixel<CYL>(p, status, ray, dev::hit_default(), false, x, y);
+        return;
+    }
     bool capped = false;
     const dev::Hit h = dev::csg_traverse<SD, ROLLED, SCU, CYL>(p.scene, ray, st, tab, lm, iter_cap, &capped);
     write_pixel<CYL>(p, status, ray, h, capped, x, y);
