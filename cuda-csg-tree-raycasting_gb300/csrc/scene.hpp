@@ -159,7 +159,7 @@ int32_t stack_class_for_depth(int32_t op_depth);
 // handful of primitives the pre-pass costs more than the pruning saves).
 bool use_prepass(int32_t n_prims);
 
-// Kernel variant for a tree: the rolled GoTo loop when the tree has more than a handful of
+// Kernel variant for a tree: the rolled GoTo loop when the tree has more than two
 // primitives, the unrolled one (which overlaps the two children's tests) for the smallest.
 // The unrolled code of the primitive tests overflows the instruction cache: 1.7-2.3x slower
 // on trees with cylinders, and since the single-leaf shortcut 14% slower on the cheese

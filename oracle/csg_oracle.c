@@ -515,7 +515,7 @@ void orc_set_short_circuit(int on) { orc_short_circuit = on ? 1 : 0; }
  * skipped, so the rest is the reference's own traversal.  Modes 1, 2, 5 and 6 leave such
  * trees unpruned.  Process-wide. */
 #define ORC_LIVE_GROUPS 1024
-#define ORC_LIVE_MIN_PRIMS 8
+#define ORC_LIVE_MIN_PRIMS 2
 static int orc_live_mode;
 static int* orc_live_lo;
 static int* orc_live_hi;

@@ -229,3 +229,28 @@ def test_render_rejects_misaligned_float4_output(csg, torch_cuda):
         rc = csg.lib().csg_render_f4(sc.h, ctypes.byref(cam.c), light, 16, 16, ctypes.c_void_p(buf.data_ptr()), None)
         assert rc == csg.CSG_OK
     torch.cuda.synchronize()
+
+
+def test_rays_without_live_leaves_vs_reference_kernel(csg, torch_cuda, refcuda):
+    """Views where most rays meet no primitive (a ray whose live mask is empty after the
+    pre-pass is written as the background without a traversal): the cheese scene seen from
+    behind the camera's usual side, from far away and at grazing angles, and random trees
+    framed so the object fills a corner; every plane against the reference kernel."""
+    from csgrt import scenes
+    from oracle import quantize_rgba8
+    light = np.float32(csg.light_dir())
+    rng = np.random.default_rng(77)
+    cases = [(scenes.config_scene_text(2, 0), d, dist) for d, dist in
+             (((0.0, 0.0, 1.0), 12.0), ((0.3, 0.95, 0.1), 2.2), ((1.0, 0.0, 0.0), 1.75))]
+    cases += [(scenes.write_text(scenes.random_tree(31000 + s, 64, 600, 10)), scenes.seeded_direction(rng),
+               float(rng.uniform(2.0, 6.0))) for s in range(4)]
+    for k, (text, d, dist) in enumerate(cases):
+        cam = csg.Camera.look_at_origin(np.array(d, float), dist).floats()
+        cam = cam.copy()
+        cam[0:3] += np.float32(0.6) * cam[9:12]  # shift the eye sideways: the object off centre
+        eng = engine_render(csg, text, cam, light, 160, 120)
+        nodes44, prims48, _ = csg.parse_tree(text)
+        ref = refcuda.render(nodes44, prims48, cam, light, 160, 120)
+        ref["rgba8"] = quantize_rgba8(ref["rgba"])
+        assert_bit_exact(eng, ref, f"sparse view {k}")
+        assert ulp_equal(eng["rgba32f"], ref["rgba"]).all(), f"sparse view {k}: float RGBA differs"

@@ -1,5 +1,5 @@
 """The scene compiler's host-side decisions (csg_tree_plan, no device work): stack class
-from the operator depth, rolled GoTo for trees of more than 8 primitives,
+from the operator depth, rolled GoTo for trees of more than 2 primitives,
 live-mask words and granularity, the fine mask of single-view renders (on request) for
 rolled trees of 1,025-2,048 leaves, the operator short-circuit for trees where Differences and
 Intersections are common, and the device layout size."""
@@ -36,7 +36,7 @@ def test_plan_matches_the_rules(csg, seed, leaves):
     assert plan["op_depth"] == _depth(tree)
     d = plan["op_depth"]
     assert plan["stack_class"] == (4 if d <= 4 else 8 if d <= 8 else 12 if d <= 12 else 16 if d <= 15 else 32)
-    assert plan["rolled"] == int(n > 8)
+    assert plan["rolled"] == int(n > 2)
     shift = 0
     while (n + (1 << shift) - 1) >> shift > 32 * 32:
         shift += 1
