@@ -50,9 +50,11 @@ struct RenderParams {
 // memory (cached in L1), which leaves their blocks' shared memory to the masks; the others
 // keep them in block shared memory (-1: always shared memory).  Measured with the operator
 // short-circuit: local stacks are 3-8% faster on trees with 27-32 mask words (1,700-4,000
-// leaves), and 1-4% slower on the cheese frame and on trees with up to ~20 words.
+// leaves); after the cone pre-pass and the empty-mask skip also 3% on the cheese frame (17
+// words) and 4-6% on batch trees of 650-700 leaves, so the threshold went from 24 words to
+// 16 (4 words: up to 4% slower on trees of ~240 leaves).
 #ifndef CSG_TILED_LOCAL_WORDS
-#define CSG_TILED_LOCAL_WORDS 24
+#define CSG_TILED_LOCAL_WORDS 16
 #endif
 // The 32-entry stack class (trees deeper than 15 operator levels) keeps its stacks in local
 // memory (a tuning knob; 0: shared memory, 48 KiB per block, four resident blocks per SM).
