@@ -2,7 +2,7 @@
 the reference's own traversal: the oracle renders seeded random trees, cheese scenes and
 the benchmark frames with and without the rule (on top of the live-leaf pruning and the
 operator short-circuit), and every plane is the same, bit for bit, while the iterations
-fall.  The rule: an operator child of at most 128 leaves with exactly one live leaf is not
+fall.  The rule: an operator child of at most 256 leaves with exactly one live leaf is not
 descended into; its result is that leaf's own (tested with its box) when every operator on
 the path down to it is a Union or a Difference entered on its left, and a Miss otherwise."""
 from __future__ import annotations
@@ -12,7 +12,7 @@ import numpy as np
 from test_live_pruning import _differ
 
 PLANES = ("hit", "t", "prim", "normal", "rgba8")
-SHORTCUT_LEAVES = 128  # the engine's kShortcutLeaves
+SHORTCUT_LEAVES = 256  # the engine's kShortcutLeaves
 
 
 def _render(oracle, nodes, prims, cam, light, w, h, shortcut, sc=True, pix=None):
