@@ -61,7 +61,7 @@ void update_vectors(csg_camera* c)
 }
 
 int render_common(const csg_scene* s, const csg_camera* cam, const float light[3], int32_t w, int32_t h,
-                  const csgrt::Planes& planes, void* stream)
+                  const csgrt::Planes& planes, void* stream, bool host_out = false)
 {
     if (!s || !cam || !light || w <= 0 || h <= 0) return CSG_E_ARG;
     if (planes.rgba32f && (reinterpret_cast<uintptr_t>(planes.rgba32f) & 15u)) return CSG_E_ARG;
@@ -69,7 +69,7 @@ int render_common(const csg_scene* s, const csg_camera* cam, const float light[3
     csgrt::Camera c;
     std::memcpy(c.v, cam, sizeof(c.v));
     const cudaError_t e = csgrt::launch_render(s->dev, s->center, c, light, w, h, planes, s->status,
-                                               static_cast<cudaStream_t>(stream));
+                                               static_cast<cudaStream_t>(stream), host_out);
     return e == cudaSuccess ? CSG_OK : CSG_E_CUDA;
 }
 
@@ -427,7 +427,7 @@ int csg_render_host(const csg_scene* s, const csg_camera* cam, const float light
     if (qe == cudaSuccess && a.type == cudaMemoryTypeHost && a.devicePointer) {
         // page-locked and mapped: the kernel stores the frame into host memory itself
         p.rgba8 = static_cast<uint32_t*>(a.devicePointer);
-        return render_common(s, cam, light_dir, w, h, p, stream);
+        return render_common(s, cam, light_dir, w, h, p, stream, true);
     }
     // pageable: a stream-ordered device frame, then a copy (which returns when done)
     const size_t bytes = (size_t)w * (size_t)h * sizeof(uint32_t);

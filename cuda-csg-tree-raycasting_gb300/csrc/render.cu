@@ -1,6 +1,6 @@
 // Single-view render kernel: RaycastKernel + LightningKernel of the reference
 // (CSGRayCasting/Graphics/RayCasting/Kernels/RaycastingKernels.cu:3-111) fused into one
-// launch, one thread per pixel, each warp an 8x4 pixel tile, shading in the traversal's
+// launch, one thread per pixel, each warp a 4x8 pixel tile, shading in the traversal's
 // epilogue.  Nothing passes through global memory between the two stages (the
 // reference round-trips a 36-byte RayHit per pixel); the only HBM traffic is the output
 // planes.  Each ray first finds the primitives it can hit at all (liveness pre-pass over
@@ -17,18 +17,28 @@ namespace csgrt {
 namespace {
 
 using pix::kThreads;
-// Warp tile (a tuning knob): CSG_TILED_WARP_W x (32 / CSG_TILED_WARP_W) pixels; a block's
-// four warps form a 2 x 2 arrangement of warp tiles.
+// Warp tile (tuning knobs, chosen per launch): W x (32 / W) pixels, W = CSG_TILED_WARP_W for
+// frames written to device memory and CSG_TILED_HOST_WARP_W for frames the kernel stores
+// into page-locked host memory; a block's four warps form a 2 x 2 arrangement of warp tiles.
+// Device frames: 4 x 8 (it was 8 x 4): with this round's pre-pass changes the cheese frame 5%
+// faster and the batch's trees as single views 2-8%, the README tree 2%; 16 x 2 was 3-8%
+// slower on the small frames.  Host frames: a warp's row of W pixels is one store of 4W bytes
+// over the host link, and 4-pixel rows took the cheese frame's end-to-end rate down 3%.
 #ifndef CSG_TILED_WARP_W
-#define CSG_TILED_WARP_W 8
+#define CSG_TILED_WARP_W 4
 #endif
-constexpr int kWarpW = CSG_TILED_WARP_W, kWarpH = 32 / CSG_TILED_WARP_W;
-constexpr int kTileW = 2 * kWarpW, kTileH = 2 * kWarpH;
-static_assert(kWarpW == 4 || kWarpW == 8 || kWarpW == 16, "warp tile width");
+#ifndef CSG_TILED_HOST_WARP_W
+#define CSG_TILED_HOST_WARP_W 8
+#endif
+static_assert(CSG_TILED_WARP_W == 4 || CSG_TILED_WARP_W == 8 || CSG_TILED_WARP_W == 16, "warp tile width");
+static_assert(CSG_TILED_HOST_WARP_W == 4 || CSG_TILED_HOST_WARP_W == 8 || CSG_TILED_HOST_WARP_W == 16,
+              "warp tile width");
+constexpr int log2_width(int w) { return w == 4 ? 2 : w == 8 ? 3 : 4; }
 
 struct RenderParams {
     pix::ViewParams view;
     int32_t tiles_x, tiles_y;  // block tiles of the view
+    int32_t tw_log2;           // warp tile: 2^tw_log2 x 2^(5 - tw_log2) pixels
     int32_t center_row;        // block row that starts first (see tile_row)
     unsigned long long* status;
     uint32_t iter_cap;
@@ -116,8 +126,9 @@ __global__ void __launch_bounds__(kThreads, ROLLED ? CSG_ROLLED_MIN_BLOCKS : CSG
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int bx = (int)(blockIdx.x % (unsigned)p.tiles_x);
     const int by = tile_row((int)(blockIdx.x / (unsigned)p.tiles_x), p.center_row, p.tiles_y);
-    const int x = bx * kTileW + (warp & 1) * kWarpW + (lane & (kWarpW - 1));
-    const int y = by * kTileH + (warp >> 1) * kWarpH + lane / kWarpW;
+    const int ww = 1 << p.tw_log2, wh = 32 >> p.tw_log2;
+    const int x = bx * 2 * ww + (warp & 1) * ww + (lane & (ww - 1));
+    const int y = by * 2 * wh + (warp >> 1) * wh + (lane >> p.tw_log2);
     __syncthreads();
     pix::render_pixel<SD, ROLLED, FINE, SCU, CYL>(p.view, p.status, p.iter_cap, x, y, x < p.view.w && y < p.view.h, st,
                                              bs, tab, frame);
@@ -195,7 +206,7 @@ cudaError_t device_tan_half_fov(float fov, float* host_out)
 
 cudaError_t launch_render(const DeviceScene& scene, const float center[3], const Camera& cam, const float light[3],
                           int32_t w, int32_t h, const Planes& out,
-                          unsigned long long* status, cudaStream_t stream)
+                          unsigned long long* status, cudaStream_t stream, bool host_out)
 {
     RenderParams p;
     p.view.scene = scene;
@@ -208,6 +219,8 @@ cudaError_t launch_render(const DeviceScene& scene, const float center[3], const
     p.view.out = out;
     p.status = status;
     p.iter_cap = iteration_cap();
+    p.tw_log2 = log2_width(host_out ? CSG_TILED_HOST_WARP_W : CSG_TILED_WARP_W);
+    const int kTileW = 2 << p.tw_log2, kTileH = 64 >> p.tw_log2;
     p.tiles_x = (w + kTileW - 1) / kTileW;
     p.tiles_y = (h + kTileH - 1) / kTileH;
     p.center_row = 0;

@@ -43,7 +43,7 @@ void set_iteration_cap(uint32_t cap);
 // of the scene's root box, sets the order in which the pixel tiles start.
 cudaError_t launch_render(const DeviceScene& scene, const float center[3], const Camera& cam, const float light[3],
                           int32_t w, int32_t h, const Planes& out,
-                          unsigned long long* status, cudaStream_t stream);
+                          unsigned long long* status, cudaStream_t stream, bool host_out = false);
 
 // tan(fov / 2) exactly as the kernels' ray generation computes it (device tanf);
 // a diagnostic for host code that restates the ray generation.
