@@ -232,6 +232,14 @@ def frame_speedup(config: int, steps: int = 10, warmup: int = 3, seed: int = 0):
     return res
 
 
+def launches_per_frame(w: int, h: int) -> int:
+    """Kernels one steady-state frame of one view launches: render_tiled, and for frames of at
+    least 32,768 block tiles of 8x16 pixels (the cost-ordered dispatch, whose gate stays open
+    on frames with long blocks, such as the cheese frame) order_count and order_scatter."""
+    tiles = ((w + 7) // 8) * ((h + 15) // 16)
+    return 3 if tiles >= 32768 else 1
+
+
 def run_engine(args):
     import torch
     import csgrt
@@ -325,7 +333,7 @@ def run_engine(args):
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "kernel_ms": {"mean": avg_launch_ms, "min": float(np.min(launch_ms)), "max": float(np.max(launch_ms))},
         "flush_ms_per_step": round((bracket_ms - total_ms) / args.steps, 4),
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * launches_per_frame(w, h),
         "e2e": {"value": round(rays * e2e_steps / e2e_s / 1e6, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 72,
                 "d2h_bytes_per_step": rays * 4,
                 "note": "csg_render_host through the C ABI: camera and light in (72 B as launch parameters), the "

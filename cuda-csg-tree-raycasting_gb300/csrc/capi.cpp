@@ -69,7 +69,7 @@ int render_common(const csg_scene* s, const csg_camera* cam, const float light[3
     csgrt::Camera c;
     std::memcpy(c.v, cam, sizeof(c.v));
     const cudaError_t e = csgrt::launch_render(s->dev, s->center, c, light, w, h, planes, s->status,
-                                               static_cast<cudaStream_t>(stream), host_out);
+                                               static_cast<cudaStream_t>(stream), host_out, &s->dispatch);
     return e == cudaSuccess ? CSG_OK : CSG_E_CUDA;
 }
 
@@ -273,6 +273,7 @@ int csg_scene_destroy(csg_scene* s)
 {
     if (!s) return CSG_E_ARG;
     int rc = CSG_OK;
+    if (csgrt::release_dispatch(s->dispatch) != cudaSuccess) rc = CSG_E_CUDA;
     if (s->dmem) {
         int prev = 0;
         cudaGetDevice(&prev);

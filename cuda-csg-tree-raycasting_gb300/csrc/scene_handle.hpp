@@ -3,6 +3,7 @@
 
 #include <cstddef>
 
+#include "render.hpp"
 #include "scene.hpp"
 
 struct csg_scene {
@@ -13,6 +14,7 @@ struct csg_scene {
     unsigned long long* status = nullptr;   // rays stopped at the traversal iteration cap
     int device = 0;
     float center[3] = {0.f, 0.f, 0.f};      // centre of the root's box (block order of single views)
+    mutable csgrt::DispatchState dispatch;  // cost-ordered block dispatch of large frames
 };
 
 namespace csgrt {

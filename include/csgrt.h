@@ -135,7 +135,13 @@ void csg_light_default(float out[3]);                         /* polar -60 deg, 
  *      fused into one launch on `stream` (a cudaStream_t; NULL = legacy default) -------- */
 /* One primary ray per pixel, Kensler single-hit CSG traversal, Phong shading.
  * `light_dir` is the DirectionalLight direction (normalised inside, as the reference
- * does).  All output pointers are device pointers owned by the caller. */
+ * does).  All output pointers are device pointers owned by the caller.
+ * Frames of at least 32,768 block tiles (8x16 pixels; 2048x2048 and larger) record each
+ * tile's render time, and the scene's next frame of the same size on the same stream
+ * starts its slowest tiles first; the output is the same, byte for byte.  The first stream
+ * that renders such a frame of a scene outside a graph capture owns this state (8 bytes per
+ * tile of device memory, allocated on that call, freed by csg_scene_destroy); frames on
+ * other streams, and frames captured into graphs, keep the fixed order. */
 int csg_render(const csg_scene* scene, const csg_camera* cam, const float light_dir[3],
                int32_t w, int32_t h, uint32_t* rgba8_dev, float* t_dev, int32_t* prim_dev,
                float* normal_dev, void* stream);
