@@ -20,7 +20,7 @@ OUT = HERE / "_build"
 LIB = OUT / "libcsgrt.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["render.cu", "noalloc.cu", "views_shapes_w2.cu", "views_shapes_w8.cu", "views_shapes_local.cu",
+CU_SOURCES = ["render.cu", "render_rec.cu", "noalloc.cu", "views_shapes_w2.cu", "views_shapes_w8.cu", "views_shapes_local.cu",
               "bench_kernels.cu"]
 CPP_SOURCES = ["scene.cpp", "capi.cpp", "batch_host.cpp", "server.cpp", "image.cpp"]
 
