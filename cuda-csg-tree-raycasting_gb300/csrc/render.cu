@@ -67,19 +67,25 @@ __device__ __forceinline__ uint32_t centre_out_tile(uint32_t k, int tiles_x, int
     const uint32_t r = k / (uint32_t)tiles_x;
     return (uint32_t)tile_row((int)r, center_row, tiles_y) << 16 | (k - r * (uint32_t)tiles_x);
 }
-__device__ __forceinline__ uint32_t tile_index(uint32_t rc, int tiles_x)
-{
-    return (rc >> 16) * (uint32_t)tiles_x + (rc & 0xffffu);
-}
 
 struct OrderParams {
-    uint32_t* cost;     // read, then cleared for the next frame's recording
+    uint32_t* cost;     // read, then (clear) cleared for the next frame's recording
     uint32_t* counts;  // [blocks][kCostClasses]
     uint32_t* order;
     float* summary;     // null, or where block 0 writes {longest block, all blocks}
     uint32_t n, chunk;  // tiles; centre-out positions per block (a multiple of kOrderThreads)
     int32_t tiles_x, tiles_y, center_row;
+    int32_t shift_x, shift_y;  // tiles the view moved since the recording: tile t costs what t - shift did
+    int32_t clear;             // no shift: order_scatter clears each entry it reads
 };
+
+// The recorded entry that stands for tile rc (row << 16 | column) of this frame.
+__device__ __forceinline__ uint32_t cost_source(uint32_t rc, const OrderParams& p)
+{
+    const int r = min(max((int)(rc >> 16) - p.shift_y, 0), p.tiles_y - 1);
+    const int c = min(max((int)(rc & 0xffffu) - p.shift_x, 0), p.tiles_x - 1);
+    return (uint32_t)r * (uint32_t)p.tiles_x + (uint32_t)c;
+}
 
 // Pass 1: each block counts the cost classes of its chunk of centre-out positions.
 __global__ void __launch_bounds__(kOrderThreads) order_count(const OrderParams p)
@@ -89,8 +95,7 @@ __global__ void __launch_bounds__(kOrderThreads) order_count(const OrderParams p
     __syncthreads();
     const uint32_t k0 = min(p.n, blockIdx.x * p.chunk), k1 = min(p.n, k0 + p.chunk);
     for (uint32_t k = k0 + threadIdx.x; k < k1; k += kOrderThreads)
-        atomicAdd(&cnt[cost_class(__ldg(p.cost + tile_index(centre_out_tile(k, p.tiles_x, p.tiles_y, p.center_row),
-                                                            p.tiles_x)))],
+        atomicAdd(&cnt[cost_class(__ldg(p.cost + cost_source(centre_out_tile(k, p.tiles_x, p.tiles_y, p.center_row), p)))],
                   1u);
     __syncthreads();
     if (threadIdx.x < kCostClasses) p.counts[blockIdx.x * kCostClasses + threadIdx.x] = cnt[threadIdx.x];
@@ -149,9 +154,9 @@ __global__ void __launch_bounds__(kOrderThreads) order_scatter(const OrderParams
         const uint32_t k = s + threadIdx.x;
         const bool in = k < k1;
         const uint32_t t = in ? centre_out_tile(k, p.tiles_x, p.tiles_y, p.center_row) : 0u;
-        const uint32_t ti = tile_index(t, p.tiles_x);
-        const int cls = in ? cost_class(p.cost[ti]) : -1;
-        if (in) p.cost[ti] = 0u;  // this kernel's last read of the entry
+        const uint32_t src = cost_source(t, p);
+        const int cls = in ? cost_class(p.cost[src]) : -1;
+        if (in && p.clear) p.cost[src] = 0u;  // src is t itself: this kernel's last read of the entry
         uint32_t rank = 0, mine = 0;
 #pragma unroll
         for (int c = 0; c < kCostClasses; ++c) {
@@ -214,7 +219,8 @@ namespace {
 
 // Sets p.cost (and p.order when the previous frame of this grid recorded its costs) for a
 // launch on `stream`, with d.mu held; leaves both null where the state is not this stream's.
-cudaError_t prepare_dispatch(DispatchState& d, RenderParams& p, uint32_t tiles, cudaStream_t stream)
+cudaError_t prepare_dispatch(DispatchState& d, RenderParams& p, uint32_t tiles, const ProjectedCentre& centre,
+                             cudaStream_t stream)
 {
     if (stream == cudaStreamPerThread) return cudaSuccess;  // one handle, a stream per host thread
     cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
@@ -320,6 +326,13 @@ cudaError_t prepare_dispatch(DispatchState& d, RenderParams& p, uint32_t tiles, 
         op.tiles_x = p.tiles_x;
         op.tiles_y = p.tiles_y;
         op.center_row = p.center_row;
+        op.shift_x = op.shift_y = 0;
+        if (centre.ok && d.rec_centre.ok) {  // follow the scene across the screen
+            const float dx = std::round(centre.x - d.rec_centre.x), dy = std::round(centre.y - d.rec_centre.y);
+            op.shift_x = (int32_t)std::max(std::min(dx, (float)(p.tiles_x - 1)), (float)(1 - p.tiles_x));
+            op.shift_y = (int32_t)std::max(std::min(dy, (float)(p.tiles_y - 1)), (float)(1 - p.tiles_y));
+        }
+        op.clear = op.shift_x == 0 && op.shift_y == 0;
         uint32_t blocks = 0;
         order_grid(tiles, &blocks, &op.chunk);
         order_count<<<blocks, kOrderThreads, 0, stream>>>(op);
@@ -331,9 +344,14 @@ cudaError_t prepare_dispatch(DispatchState& d, RenderParams& p, uint32_t tiles, 
             if (e != cudaSuccess) return e;
             d.summary_pending = true;
         }
+        if (!op.clear) {  // read through the shift: cleared here instead
+            e = cudaMemsetAsync(d.cost, 0, tiles * sizeof(uint32_t), stream);
+            if (e != cudaSuccess) return e;
+        }
         p.order = d.order;
     }
     d.costs_valid = false;  // until this launch has been issued
+    d.rec_centre = centre;
     p.cost = d.cost;
     return cudaSuccess;
 }
@@ -359,23 +377,32 @@ cudaError_t launch_render(const DeviceScene& scene, const float center[3], const
     const int kTileW = 2 << p.tw_log2, kTileH = 64 >> p.tw_log2;
     p.tiles_x = (w + kTileW - 1) / kTileW;
     p.tiles_y = (h + kTileH - 1) / kTileH;
+    // the pixel of the scene's centre (Raycaster's ray generation inverted: nx = (2 u - 1)
+    // (w / h) tan(fov / 2), ny = (1 - 2 v) tan(fov / 2), u = (x + 0.5) / (w - 1),
+    // v = (y + 0.5) / (h - 1)): its row starts the centre-out order (the middle row if the
+    // centre is not in front of the camera), and the cost-ordered dispatch follows it
+    ProjectedCentre centre;
     p.center_row = 0;
-    if (CSG_TILED_CENTER_OUT) {
-        // the pixel row of the scene's centre (Raycaster's ray generation inverted:
-        // ny = (1 - 2 v) tan(fov / 2), v = (y + 0.5) / (h - 1)); the middle row if it is not
-        // in front of the camera
+    {
         const float* c = cam.v;
         const float vx = center[0] - c[0], vy = center[1] - c[1], vz = center[2] - c[2];
         const float z = vx * c[6] + vy * c[7] + vz * c[8];
         const float thf = std::tan(0.5f * c[5]);
         float row = 0.5f * (float)h;
         if (z > 0.f && thf > 0.f) {
+            const float nx = (vx * c[9] + vy * c[10] + vz * c[11]) / z;
             const float ny = (vx * c[12] + vy * c[13] + vz * c[14]) / z;
             row = 0.5f * (1.f - ny / thf) * (float)(h - 1) - 0.5f;
+            const float col = 0.5f * (1.f + nx / (thf * (float)w / (float)h)) * (float)(w - 1) - 0.5f;
+            centre.ok = std::isfinite(col) && std::isfinite(row) && std::fabs(col) < 1e7f && std::fabs(row) < 1e7f;
+            centre.x = col / (float)kTileW;
+            centre.y = row / (float)kTileH;
         }
-        if (!(row >= 0.f)) row = 0.f;  // also NaN
-        if (row > (float)(h - 1)) row = (float)(h - 1);
-        p.center_row = std::min((int)row / kTileH, p.tiles_y - 1);
+        if (CSG_TILED_CENTER_OUT) {
+            if (!(row >= 0.f)) row = 0.f;  // also NaN
+            if (row > (float)(h - 1)) row = (float)(h - 1);
+            p.center_row = std::min((int)row / kTileH, p.tiles_y - 1);
+        }
     }
     p.order = nullptr;
     p.cost = nullptr;
@@ -384,7 +411,7 @@ cudaError_t launch_render(const DeviceScene& scene, const float center[3], const
     if (dispatch && CSG_DISPATCH_MIN_TILES > 0 && tiles >= (uint32_t)CSG_DISPATCH_MIN_TILES && p.tiles_x < 65536 &&
         p.tiles_y < 65536) {
         lock = std::unique_lock<std::mutex>(dispatch->mu);
-        const cudaError_t e = prepare_dispatch(*dispatch, p, tiles, stream);
+        const cudaError_t e = prepare_dispatch(*dispatch, p, tiles, centre, stream);
         if (e != cudaSuccess) return e;
     }
     const cudaError_t e = p.cost ? launch_tiled<true>(p, stream) : launch_tiled<false>(p, stream);

@@ -39,6 +39,12 @@ constexpr uint32_t kIterCap = 1u << 20;
 uint32_t iteration_cap();
 void set_iteration_cap(uint32_t cap);
 
+// Where the scene's centre falls in a frame, in block tiles (ok: in front of the camera).
+struct ProjectedCentre {
+    bool ok = false;
+    float x = 0.f, y = 0.f;
+};
+
 // Per-scene state of the cost-ordered block dispatch of large frames (launch_render).  The
 // render kernel records each block's duration; the next frame of the same scene, on the same
 // tile grid and stream, starts its tiles longest first.  One stream owns the state (the first
@@ -54,6 +60,7 @@ struct DispatchState {
     cudaStream_t stream = nullptr;
     int slots = 0;                                   // SMs x 6 resident blocks
     int32_t tiles_x = 0, tiles_y = 0, tw_log2 = -1;  // the grid `cost` was recorded on
+    ProjectedCentre rec_centre;                      // and where the scene's centre was
     bool costs_valid = false;
     uint32_t* cost = nullptr;    // per tile (row-major): SM cycles from the block's start to its end
     uint32_t* order = nullptr;   // the k-th block to start renders tile order[k]

@@ -1,5 +1,6 @@
 """The cost-ordered dispatch's order (csrc/render.cu: order_grid, order_count, order_scatter),
-restated in numpy: the positions the two kernels compute (a class's start, plus the same
+restated in numpy (with the view shift that makes a tile read the recorded cost of the tile
+it came from): the positions the two kernels compute (a class's start, plus the same
 class's tiles in earlier blocks, which each order_scatter block sums from order_count's
 per-block counts, plus the same class's earlier tiles inside the block) form a permutation
 of the tiles, longest class first, centre-out order within a class, on grids from one tile
@@ -35,7 +36,7 @@ def order_grid(n):
     return g, (per + THREADS - 1) // THREADS * THREADS
 
 
-def dispatch_order(tiles_x, tiles_y, center_row, cost):
+def dispatch_order(tiles_x, tiles_y, center_row, cost, shift_x=0, shift_y=0):
     n = tiles_x * tiles_y
     g, chunk = order_grid(n)
     assert g <= BLOCKS_MAX and chunk % THREADS == 0 and g * chunk >= n
@@ -43,7 +44,9 @@ def dispatch_order(tiles_x, tiles_y, center_row, cost):
     row = tile_row(k // tiles_x, center_row, tiles_y)
     tile = row * tiles_x + k % tiles_x                 # row-major index of position k
     packed = (row << 16) | (k % tiles_x)               # what order[] holds
-    cls = cost_class(cost[tile])
+    # cost_source: the recorded entry standing for each tile once the view moved by the shift
+    src = (np.clip(row - shift_y, 0, tiles_y - 1) * tiles_x + np.clip(k % tiles_x - shift_x, 0, tiles_x - 1))
+    cls = cost_class(cost[src])
     block = k // chunk
     counts = np.zeros((g, CLASSES), np.int64)
     np.add.at(counts, (block, cls), 1)
@@ -64,19 +67,21 @@ def dispatch_order(tiles_x, tiles_y, center_row, cost):
     assert pos.min() >= 0 and pos.max() < n
     order = np.full(n, -1, np.int64)
     order[pos] = packed
-    return order, tile, cls, k
+    return order, tile, cls, k, src
 
 
-@pytest.mark.parametrize("tiles_x,tiles_y,center_row", [
-    (1, 1, 0), (7, 3, 1), (33, 17, 16), (100, 61, 0), (100, 61, 60), (480, 135, 67), (240, 270, 135),
-    (13, 5000, 2500), (257, 257, 3), (512, 128, 64)])
-def test_positions_are_a_stable_class_order(tiles_x, tiles_y, center_row):
+@pytest.mark.parametrize("tiles_x,tiles_y,center_row,shift_x,shift_y", [
+    (1, 1, 0, 0, 0), (7, 3, 1, 0, 0), (33, 17, 16, 5, -3), (100, 61, 0, 0, 0), (100, 61, 60, -99, 60),
+    (480, 135, 67, 23, 0), (240, 270, 135, 0, 0), (13, 5000, 2500, 0, -4999), (257, 257, 3, 1, 1),
+    (512, 128, 64, -17, 2)])
+def test_positions_are_a_stable_class_order(tiles_x, tiles_y, center_row, shift_x, shift_y):
     rng = np.random.default_rng(tiles_x * 7919 + tiles_y)
     n = tiles_x * tiles_y
     for cost in (np.exp(rng.uniform(0, 22, n)).astype(np.uint64).clip(0, 2 ** 32 - 1),
                  np.zeros(n, np.uint64), np.full(n, 2 ** 32 - 1, np.uint64),
                  rng.integers(0, 2 ** 32, n, dtype=np.uint64)):
-        order, tile, cls, k = dispatch_order(tiles_x, tiles_y, center_row, cost)
+        order, tile, cls, k, src = dispatch_order(tiles_x, tiles_y, center_row, cost, shift_x, shift_y)
+        assert src.min() >= 0 and src.max() < n                     # reads stay inside the array
         assert (order >= 0).all()
         rows, cols = order >> 16, order & 0xFFFF
         assert rows.max() < tiles_y and cols.max() < tiles_x
@@ -84,7 +89,9 @@ def test_positions_are_a_stable_class_order(tiles_x, tiles_y, center_row):
         assert (np.sort(raster) == np.arange(n)).all()               # every tile once
         pos_of = np.empty(n, np.int64)
         pos_of[tile] = k                                             # centre-out position of a tile
-        c = cost_class(cost[raster])
+        src_of = np.empty(n, np.int64)
+        src_of[tile] = src
+        c = cost_class(cost[src_of[raster]])
         assert (np.diff(c) >= 0).all()                               # longest class first
         same = np.diff(c) == 0
         assert (np.diff(pos_of[raster])[same] > 0).all()             # centre-out within a class
