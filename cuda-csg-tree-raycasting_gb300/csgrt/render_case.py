@@ -7,6 +7,12 @@ enough to run under a profiler.
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2 --local-stacks
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scenes 32 --repeat 2 --noalloc
     python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --batch-scene 191 --view-width 1024
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 2 --time --repeat 10 --turn 0.05
+    python cuda-csg-tree-raycasting_gb300/csgrt/render_case.py --config 1 --size 3840x2160 --time --sync
+
+--time measures a sequence of frames (CUDA events on the stream, 3 warm-up frames, the L2
+flushed by a 256 MiB write before each frame) and prints the mean as one JSON line: how the
+cost-ordered dispatch of large frames is measured against a build without it (CSGRT_LIB).
 
 Configurations: 1 the README tree at 1280x720, 2 the 512-sphere cheese at 3840x2160,
 3 a random tree at 1920x1080 (seeded), as in bench.py.
@@ -14,6 +20,7 @@ Configurations: 1 the README tree at 1280x720, 2 the 512-sphere cheese at 3840x2
 from __future__ import annotations
 
 import argparse
+import json
 import sys
 from pathlib import Path
 
@@ -42,6 +49,11 @@ def main(argv=None):
                     help="with --batch-scenes: one plain csg_render_views_noalloc launch (no graph) per repeat")
     ap.add_argument("--png", default="", help="write the (single-view) frame as PNG")
     ap.add_argument("--ppm", default="", help="write the (single-view) frame as PPM")
+    ap.add_argument("--size", default="", help="single view: render at WxH instead of the view's size")
+    ap.add_argument("--turn", type=float, default=0.0, help="single view: yaw step per frame in radians")
+    ap.add_argument("--away", action="store_true", help="single view: camera turned away (every ray misses)")
+    ap.add_argument("--time", action="store_true", help="single view: time the frames (see above)")
+    ap.add_argument("--sync", action="store_true", help="with --time: synchronise the stream after each frame")
     a = ap.parse_args(argv)
 
     import torch
@@ -79,11 +91,44 @@ def main(argv=None):
         view = next((v for v in vs if v.w == a.view_width), vs[0])
     else:
         text, view = scenes.config_scene_text(a.config, a.seed), scenes.config_views(a.config, a.seed)[0]
+    camf = np.array(view.camera, np.float32).copy()
+    if a.away:
+        camf[6:9] *= -1.0  # forward reversed
+    if a.size:
+        w, h = (int(x) for x in a.size.lower().split("x"))
+        view = scenes.View(camf, view.light, w, h)
     sc = csgrt.Scene(text, exact_boxes=a.exact)
-    cam = csgrt.Camera.from_floats(view.camera)
+
+    def camera(i):
+        c = csgrt.Camera.from_floats(camf)
+        if a.turn:
+            c.rotate(0.0, a.turn * i)
+        return c
+
     out = torch.empty(view.w * view.h, dtype=torch.int32, device="cuda")
-    for _ in range(a.repeat):
-        sc.render_ptrs(cam, view.light, view.w, view.h, rgba8=out.data_ptr())
+    if a.time:
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+        st = torch.cuda.current_stream()
+        ev = []
+        for i in range(a.repeat + 3):
+            c = camera(i)
+            flush.zero_()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(st)
+            sc.render_ptrs(c, view.light, view.w, view.h, rgba8=out.data_ptr(), stream=st.cuda_stream)
+            t1.record(st)
+            ev.append((t0, t1))
+            if a.sync:
+                st.synchronize()
+        torch.cuda.synchronize()
+        ms = [t0.elapsed_time(t1) for t0, t1 in ev[3:]]
+        print(json.dumps({"width": view.w, "height": view.h, "frames": len(ms), "turn": a.turn, "away": a.away,
+                          "sync": a.sync, "ms_mean": round(float(np.mean(ms)), 4),
+                          "ms_min": round(float(np.min(ms)), 4), "lib": getattr(csgrt.lib(), "_name", "")}))
+    else:
+        cam = camera(0)
+        for _ in range(a.repeat):
+            sc.render_ptrs(cam, view.light, view.w, view.h, rgba8=out.data_ptr())
     torch.cuda.synchronize()
     capped = sc.check()
     print("view", view.w, view.h, sc.info(), "capped rays", capped)
