@@ -1,4 +1,4 @@
-// Per-pixel body shared by the single-view kernel (render.cu) and the persistent
+// Per-pixel body shared by the single-view kernel (render_tiled.cuh) and the persistent
 // view-table kernel (views_kernel.cuh): shared-memory layout of a block, and one pixel's
 // ray generation, liveness pre-pass, traversal, details, shading and output planes.
 #pragma once

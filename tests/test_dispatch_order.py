@@ -15,7 +15,7 @@ THREADS, CLASSES, BLOCKS_MAX, KEY_TOP = 256, 32, 256, 45
 
 
 def tile_row(k, c, n):
-    """render.cu tile_row, vectorised over k."""
+    """tile_row (render_tiled.cuh), vectorised over k."""
     k = np.asarray(k, np.int64)
     m = min(c, n - 1 - c)
     near = np.where(k & 1, c - ((k + 1) >> 1), c + (k >> 1))
