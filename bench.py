@@ -330,6 +330,10 @@ def run_engine(args):
                    "boxes": "exact (CSG_SCENE_EXACT_BOXES, not the reference's output)" if args.exact
                    else "reference",
                    "l2": "flushed before every step by a 256 MiB device write, between the steps' events",
+                   "block_order": ("cost-ordered: each step runs order_count and order_scatter on the previous "
+                                   "step's recorded block durations, then render_tiled; all three inside the "
+                                   "step's events" if launches_per_frame(w, h) == 3
+                                   else "fixed, centre-out rows (frame under 32,768 tiles)"),
                    "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU"},
         "kernel_ms": {"mean": avg_launch_ms, "min": float(np.min(launch_ms)), "max": float(np.max(launch_ms))},
         "flush_ms_per_step": round((bracket_ms - total_ms) / args.steps, 4),
